@@ -1,0 +1,399 @@
+"""RK2 steps/s of the GB300-native Gturbo3D step at 512^3.
+
+Workload (the roofline configuration): 512^3 periodic box [0,2pi)^3, nu = 2e-4,
+Omega = 5, dt = 1e-3, 3D3C forcing on 2 <= |k| <= 3 at injection 0.1 (seed 2),
+2/3 dealiasing, initial field E(k) ~ k^4 exp(-2 (k/3)^2) normalised to E = 0.5
+(synthetic, seeded).  One step = one RK2 integrating-factor step
+(main.f90:121-150) in dt2 = dt/2 mode: two nonlinear terms (18 3D real FFTs),
+both integrating-factor updates and the forcing.
+
+  value      mixed-form (FP32 state/FFTs, FP64 exponentials, forcing
+             normalisation and reductions) steps/s, state resident in HBM
+  e2e        the same through the C-ABI call a Fortran driver makes,
+             gt_rk2_step(h, 1, &seed) with the host-drawn forcing copied in
+             each step and the energy (gt_energy) read back each step
+  fp64       the plain FP64 form's steps/s on the same workload
+  rel_energy_err  |E_mixed - E_fp64| / E_fp64 after --energy-steps steps
+
+The working set (12 fields, 6.6 GB mixed / 13 GB FP64) is far larger than the
+129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+FP64 NumPy/SciPy restatement in oracle/, scipy.fft with all host threads) on
+a bounded sample and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 512
+PHYS = dict(nu=2e-4, omega=5.0, dt=1e-3)
+SEED = 2
+INJECTION = 0.1
+METRIC = "RK2 steps/s @512^3 (mixed FP32/FP64 form; FP64 plain form and rel. energy error reported beside)"
+UNIT = "steps/s"
+
+
+def workload_config(extra=None):
+    c = {"workload": "rk2_step_512cubed_roofline_config", "grid": [N, N, N], "nu": PHYS["nu"],
+         "omega": PHYS["omega"], "dt": PHYS["dt"], "forcing": "3d3c k in (1.999,3] injection 0.1",
+         "seed": SEED, "dt2_mode": "rk2", "truncate": 1,
+         "l2_flush": "not needed: 12-field working set (6.6 GB) >> 129 MB L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_sim(precision, device, seed_offset=0):
+    import gturbo3d_gb300 as g
+    p = g.make_params(N, precision=precision, forcing="3d3c", device=device, **PHYS)
+    p.famp = g.forcing_amplitude(INJECTION, p)
+    return g.Simulation(p)
+
+
+def initial_state(rank: int):
+    from gturbo3d_gb300.synth import initial_potential
+    return initial_potential(N, N, N, SEED + rank)
+
+
+def measured_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return None
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary
+    (profiles/ncu_traffic.txt: 'kernel precision bytes_per_launch workload')."""
+    out = {}
+    f = ROOT / "profiles" / "ncu_traffic.txt"
+    if not f.exists():
+        return out
+    for ln in f.read_text().splitlines():
+        if not ln.strip() or ln.startswith("#"):
+            continue
+        parts = ln.split()
+        if len(parts) >= 3:
+            try:
+                out[(parts[0], parts[1])] = float(parts[2])
+            except ValueError:
+                pass
+    return out
+
+
+def time_steps(sim, steps, warmup, seed, torch, profile=False):
+    """Device-resident timing: CUDA events on the library's stream."""
+    stream = torch.cuda.ExternalStream(sim.stream)
+    s = seed
+    s = sim.step(warmup, s)
+    torch.cuda.synchronize()
+    if profile:
+        sim.profile(True)
+        sim.profile_read()
+    n0 = sim.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s = sim.step(steps, s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = sim.launch_count() - n0
+    prof = sim.profile_read() if profile else None
+    if profile:
+        sim.profile(False)
+    return ms, launches, prof, s
+
+
+def time_e2e(sim, steps, seed, torch):
+    """Through the C-ABI with host buffers: per step gt_rk2_step (host-drawn
+    forcing copied to the device) and gt_energy (energy read back)."""
+    import numpy as np
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = seed
+    e = []
+    for _ in range(steps):
+        s = sim.step(1, s)
+        e.append(sim.energy())
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return dt, np.array(e), s
+
+
+def cpu_baseline(budget_s=30.0):
+    """The FP64 NumPy/SciPy restatement (oracle/) on the host cores: one RK2
+    step on the largest grid of 512/256/128 whose step fits the budget,
+    reported as 512^3-equivalent steps/s by the FFT flop ratio
+    N^3 log2 N^3 (a bounded sample, scaled to the metric's unit)."""
+    import numpy as np
+    from oracle.gturbo_oracle import Oracle, Params
+    from gturbo3d_gb300.synth import initial_potential, forcing_amplitude
+    import scipy.fft as sfft
+    cores = os.cpu_count() or 1
+    est = None
+    for n in (128, 256, 512):
+        if est is not None and est * 8 * 1.15 > budget_s:
+            break
+        p = Params(nx=n, ny=n, nz=n, forcing="3d3c", **PHYS)
+        o = Oracle(p, workers=cores)
+        p.famp = forcing_amplitude(INJECTION, o.fm.nf)
+        o = Oracle(p, workers=cores)
+        b = initial_potential(n, n, n, SEED)
+        with sfft.set_workers(cores):
+            t0 = time.perf_counter()
+            o.rk2_step(b, SEED)
+            est = time.perf_counter() - t0
+        grid, t_step = n, est
+        del b, o
+    scale = (N ** 3 * math.log2(N ** 3)) / (grid ** 3 * math.log2(grid ** 3))
+    return {"value": 1.0 / (t_step * scale), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one FP64 oracle RK2 step at {grid}^3 took {t_step:.2f} s on {cores} threads "
+                      f"(scipy.fft workers={cores}); scaled x{scale:.1f} to 512^3 by N^3 log2 N^3"}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import scipy.fft as sfft
+    from oracle.gturbo_oracle import Oracle, Params
+    from gturbo3d_gb300.synth import initial_potential, forcing_amplitude
+    cores = os.cpu_count() or 1
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    # pick the sample grid: largest of 64/128/256/512 whose step fits the per-step budget
+    grid, t_est = 64, None
+    for n in (64, 128, 256, 512):
+        p = Params(nx=n, ny=n, nz=n, forcing="3d3c", **PHYS)
+        o = Oracle(p, workers=cores)
+        p.famp = forcing_amplitude(INJECTION, o.fm.nf)
+        o = Oracle(p, workers=cores)
+        b = initial_potential(n, n, n, SEED)
+        with sfft.set_workers(cores):
+            t0 = time.perf_counter()
+            o.rk2_step(b, SEED)
+            t = time.perf_counter() - t0
+        grid, t_est = n, t
+        if t * 8 * 1.15 > budget:
+            break
+    p = Params(nx=grid, ny=grid, nz=grid, forcing="3d3c", **PHYS)
+    o = Oracle(p, workers=cores)
+    p.famp = forcing_amplitude(INJECTION, o.fm.nf)
+    o = Oracle(p, workers=cores)
+    b = initial_potential(grid, grid, grid, SEED)
+    s = SEED
+    with sfft.set_workers(cores):
+        for _ in range(args.warmup):
+            b, s, _ = o.rk2_step(b, s)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b, s, _ = o.rk2_step(b, s)
+        dt = time.perf_counter() - t0
+    scale = (N ** 3 * math.log2(N ** 3)) / (grid ** 3 * math.log2(grid ** 3))
+    value = args.steps / (dt * scale)
+    sample = (f"{args.steps} FP64 oracle RK2 steps at {grid}^3 on {cores} threads took {dt:.2f} s; "
+              f"scaled x{scale:.1f} to 512^3 by N^3 log2 N^3")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field)",
+            "config": workload_config({"sample_grid": [grid] * 3}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    device = local if ws > 1 else 0
+
+    b0 = initial_state(rank)
+    seed = SEED + rank
+
+    # --- mixed form: the headline ---------------------------------------------
+    sim = make_sim("mixed", device)
+    sim.set_state(b0)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    ms, launches, prof, _ = time_steps(sim, args.steps, args.warmup, seed, torch, profile=True)
+    clk = clocks.stop()
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    value = ws * args.steps / (ms_max / 1e3)
+
+    # --- e2e through the C-ABI with host buffers ------------------------------
+    sim.set_state(b0)
+    e2e_s, _, _ = time_e2e(sim, args.steps, seed, torch)
+    te = torch.tensor([e2e_s], device="cuda")
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = ws * args.steps / float(te.item())
+    nf = len(__import__("gturbo3d_gb300").forced_modes(sim.params).ix)
+    h2d = (nf + 10) * 64            # ForceEntry records of one step (incl. conjugate partners)
+    d2h = 3 * 8                     # three energy components
+    # --- energy error mixed vs FP64 after --energy-steps steps ----------------
+    rel_err = None
+    fp64_value = None
+    if args.energy_steps > 0 or args.fp64_steps > 0:
+        sim64 = make_sim("fp64", device)
+        sim64.set_state(b0)
+        ms64, _, prof64, _ = time_steps(sim64, args.fp64_steps, 1, seed, torch, profile=True)
+        fp64_value = args.fp64_steps / (ms64 / 1e3)
+        if args.energy_steps > 0:
+            sim64.set_state(b0)
+            sim64.step(args.energy_steps, seed)
+            sim.set_state(b0)
+            sim.step(args.energy_steps, seed)
+            e64, e32 = sim64.energy(), sim.energy()
+            rel_err = abs(e32 - e64) / e64
+        sim64.close()
+
+    # --- roofline of the dominant kernel --------------------------------------
+    peaks = measured_peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    nh = N // 2 + 1
+    field_bytes = N * N * nh * 8          # one FP32 complex field, algorithmic (no row padding)
+    roof = None
+    if dom:
+        name, (nl, tms) = dom
+        per_launch_bytes = 9 * field_bytes   # every pass moves 9 fields
+        avg_s = tms / nl / 1e3
+        achieved = per_launch_bytes / avg_s / 1e9
+        traffic = ncu_traffic().get((name, "mixed"))
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3,
+                "kernels": {k: {"launches": v[0], "ms_total": v[1]} for k, v in prof.items()}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 2 + rank)",
+            "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps},
+            "rel_energy_err_mixed_vs_fp64": rel_err, "energy_steps": args.energy_steps,
+            "roofline": roof, "clocks": clk}
+    sim.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--energy-steps", type=int, default=100)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

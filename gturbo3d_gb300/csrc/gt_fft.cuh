@@ -1,0 +1,165 @@
+// Device FFT building blocks: complex arithmetic, radix-2/4/8 butterflies and
+// a Stockham line transform in which each thread holds 8 elements.
+//
+// Line transform convention.  A line of length L = 2^lgL (8 <= L <= 1024) is
+// transformed by L/8 threads t = 0..L/8-1.  On entry thread t holds
+// v[i] = x[t + i L/8] (i = 0..7); on exit it holds X[t + i L/8] in natural
+// order, so the first stage can be fed from global memory and the last stage
+// can store to global memory without a shared-memory round trip.  Stages use
+// radix 8 while at least three factors of two remain, then one radix-4 or
+// radix-2 stage.  A stage with radix r and Ns = product of earlier radices does
+// 8/r butterflies b = t + m L/8 per thread; butterfly b reads registers
+// m + j (8/r), multiplies input j by W_{Ns r}^{j (b mod Ns)} and writes output
+// j to position (b div Ns) Ns r + (b mod Ns) + j Ns.
+//
+// SIGN = -1 is the forward transform X_k = sum x_n e^{-2 pi i k n / L}
+// (numpy and cuFFT convention); SIGN = +1 the unnormalised inverse.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace gt {
+
+template <typename R> struct CplxOf;
+template <> struct CplxOf<float> { using type = float2; };
+template <> struct CplxOf<double> { using type = double2; };
+template <typename R> using Cplx = typename CplxOf<R>::type;
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+
+// a * W4^{SIGN}: the forward transform multiplies by -i, the inverse by +i.
+template <int SIGN, typename C> __device__ __forceinline__ C rot90(C a) {
+  return SIGN < 0 ? C{a.y, -a.x} : C{-a.y, a.x};
+}
+
+// a * w (forward) or a * conj(w) (inverse) for a table entry w = e^{-2 pi i m/L}.
+template <int SIGN, typename C> __device__ __forceinline__ C twmul(C a, C w) {
+  if (SIGN < 0) return C{a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x};
+  return C{a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y};
+}
+
+template <typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+  const C t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft4(C& x0, C& x1, C& x2, C& x3) {
+  const C s0 = cadd(x0, x2), d0 = csub(x0, x2);
+  const C s1 = cadd(x1, x3), d1 = rot90<SIGN>(csub(x1, x3));
+  x0 = cadd(s0, s1);
+  x2 = csub(s0, s1);
+  x1 = cadd(d0, d1);
+  x3 = csub(d0, d1);
+}
+
+// 8-point DFT in natural order: two 4-point DFTs of the even and odd inputs,
+// the odd outputs rotated by W8^q, then one radix-2 layer.
+template <int SIGN, typename R, typename C> __device__ __forceinline__ void dft8(C v[8]) {
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<SIGN>(e0, e1, e2, e3);
+  dft4<SIGN>(o0, o1, o2, o3);
+  const R c = (R)0.70710678118654752440;
+  if (SIGN < 0) {  // W8 = (1 - i)/sqrt2, W8^3 = (-1 - i)/sqrt2
+    o1 = C{c * (o1.x + o1.y), c * (o1.y - o1.x)};
+    o2 = C{o2.y, -o2.x};
+    o3 = C{c * (o3.y - o3.x), -c * (o3.x + o3.y)};
+  } else {         // W8 = (1 + i)/sqrt2, W8^3 = (-1 + i)/sqrt2
+    o1 = C{c * (o1.x - o1.y), c * (o1.x + o1.y)};
+    o2 = C{-o2.y, o2.x};
+    o3 = C{-c * (o3.x + o3.y), c * (o3.x - o3.y)};
+  }
+  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+
+// Shared-memory addressing of one line.
+//  Strided: element e of column x of an [L][ld] tile lives at e*ld + x.
+struct StridedIdx {
+  int ld, x;
+  __device__ __forceinline__ int operator()(int e) const { return e * ld + x; }
+};
+//  Contiguous with one padding slot every 2^sh elements (bank-conflict
+//  avoidance for the strided Stockham writes of the first stage).
+struct PaddedIdx {
+  int off, sh;
+  __device__ __forceinline__ int operator()(int e) const { return off + e + (e >> sh); }
+};
+
+// One line transform; every thread of the CTA must call this the same number
+// of times (it synchronises the CTA between stages).  The line's shared
+// scratch `sm` (addressed by `idx`) may be overwritten.
+template <int SIGN, typename R, typename Idx>
+__device__ __forceinline__ void fft_line(Cplx<R> v[8], int t, int lgL,
+                                         const Cplx<R>* __restrict__ tw, Cplx<R>* sm, Idx idx) {
+  using C = Cplx<R>;
+  const int T = 1 << (lgL - 3);
+  int rem = lgL;
+  int lgNs = 0;
+  while (true) {
+    const int lr = rem >= 3 ? 3 : rem;
+    rem -= lr;
+    const bool last = (rem == 0);
+    const int Ns = 1 << lgNs;
+    if (lr == 3) {
+      const int k = t & (Ns - 1);
+      if (lgNs > 0) {
+        const int step = k << (lgL - lgNs - 3);
+#pragma unroll
+        for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tw[j * step]));
+      }
+      dft8<SIGN, R>(v);
+      if (!last) {
+        const int base = ((t >> lgNs) << (lgNs + 3)) + k;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sm[idx(base + (j << lgNs))] = v[j];
+      }
+    } else if (lr == 2) {
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const int b = t + m * T;
+        const int k = b & (Ns - 1);
+        if (lgNs > 0) {
+          const int step = k << (lgL - lgNs - 2);
+          v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tw[step]));
+          v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[2 * step]));
+          v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tw[3 * step]));
+        }
+        dft4<SIGN>(v[m], v[m + 2], v[m + 4], v[m + 6]);
+        if (!last) {
+          const int base = ((b >> lgNs) << (lgNs + 2)) + k;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) sm[idx(base + (j << lgNs))] = v[m + 2 * j];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int b = t + m * T;
+        const int k = b & (Ns - 1);
+        if (lgNs > 0) {
+          const int step = k << (lgL - lgNs - 1);
+          v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[step]));
+        }
+        dft2(v[m], v[m + 4]);
+        if (!last) {
+          const int base = ((b >> lgNs) << (lgNs + 1)) + k;
+          sm[idx(base)] = v[m];
+          sm[idx(base + Ns)] = v[m + 4];
+        }
+      }
+    }
+    if (last) break;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
+    __syncthreads();
+    lgNs += lr;
+  }
+}
+
+}  // namespace gt

@@ -1,0 +1,145 @@
+// Internal declarations shared by the host set-up code (gt_host.cpp), the
+// kernels (gt_kernels.cu) and the C-ABI (gt_capi.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gturbo_gb.h"
+
+namespace gt {
+
+constexpr double kPiRef = 3.14159265358979323846;          // defk.f90:24
+constexpr double kPi2_3d3c = 2.0 * 3.14159265358979323846; // forcing_3d3c.f90:21
+constexpr double kPi2_2d2c = 2.0 * 3.14159265358979;       // forcing_2d2c.f90:20
+constexpr int32_t kLcgMul = 69069;                          // forcing_3d3c.f90:89
+constexpr int32_t kLcgMask = 0x7FFFFFFF;                    // forcing_3d3c.f90:88
+
+// Wavenumber tables and derived per-mode data, as defk builds them
+// (defk.f90:13-91), plus the truncation boundary and forced-mode list.
+struct HostTables {
+  int nx = 0, ny = 0, nz = 0, nh = 0;
+  std::vector<double> fkx, fky, fkz, fkxs, fkys, fkzs;
+  std::vector<int32_t> jc, kc;                 // 0-based conjugate indices
+  double fkxsmax = 0, fkysmax = 0, fkzsmax = 0, rtrunc2 = 0;
+  // emk = exp(-0.5 dt (nu k2^alpnu + mu k2^alpmu)), = 1 at k2 = 0.
+  bool emk_by_k2 = false;                      // integer wavenumbers: emk indexed by k2
+  std::vector<double> emk_k2;                  // [k2max + 1] when emk_by_k2
+  std::vector<double> emk_full;                // [nz][ny][nh] otherwise
+  // Truncation: mode (ix, iy, iz) survives trunc iff ix < xcut[iz*ny + iy]
+  // (and it is not (0,0,0)).  xcut = nh everywhere when truncate = 0.
+  std::vector<int32_t> xcut;
+  // Forced modes in the reference's order.
+  std::vector<int32_t> fix, fiy, fiz;
+  std::vector<double> ff;
+  double inpe = 0, inpz = 0;
+};
+
+// One scatter-add of the forcing: b_c(z, y, x) += inc[2c] + i inc[2c+1] for
+// every component c whose bit is set in mask.
+struct ForceEntry {
+  int32_t z, y, x, mask;
+  double inc[6];
+};
+
+int build_tables(const gt_params& p, HostTables& t);
+double emk_value(const gt_params& p, double k2);
+// rann (forcing_3d3c.f90:82-93): advance state, return REAL*4 value.
+float rann(int32_t& irand);
+// Appends one step's forcing entries, in the reference's order, advancing
+// the seed exactly as forcing_3d3c.f90:26-72 / forcing_2d2c.f90:27-48 do.
+void draw_forcing(const gt_params& p, const HostTables& t, int32_t& seed,
+                  std::vector<ForceEntry>& out);
+bool entries_unique(const ForceEntry* e, size_t n);
+
+// ---- device side --------------------------------------------------------
+
+// Layout of one spectral field on the device: [nz][ny][nhp] complex with the
+// row length nhp padded to a multiple of 128 bytes.
+struct Geom {
+  int nx, ny, nz, nh, nhp;
+  int lnx, lny, lnz;  // log2 of nx, ny, nz
+  size_t field_elems() const { return (size_t)nz * ny * nhp; }
+};
+
+// Device-resident tables, in the working precision R (float or double)
+// except where noted.
+template <typename R>
+struct DevTables {
+  const R* fkx;    // [nh]
+  const R* fky;    // [ny]
+  const R* fkz;    // [nz]
+  const R* fkxs;   // [nh]
+  const R* fkys;   // [ny]
+  const R* fkzs;   // [nz]
+  const R* emk;    // by k2 (emk_by_k2) or [nz][ny][nh]
+  int emk_by_k2;
+  const int32_t* xcut;  // [nz][ny]
+  const void* twx;      // twiddles exp(-2 pi i m / nx), m < nx  (complex R)
+  const void* twy;      // ny
+  const void* twz;      // nz
+  R omega, dt, dt2, scale;  // scale = 1/(nx ny nz)
+  int truncate;
+};
+
+enum NltMode { kNltOnly = 0, kStage1 = 1, kStage2 = 2 };
+
+// Work buffers: w[0..5] hold u_x,u_y,u_z,w_x,w_y,w_z between passes; after
+// the x-pass w[0..2] hold u x w.
+template <typename R>
+struct Fields {
+  void* b[3];
+  void* c[3];
+  void* w[6];
+};
+
+// Launchers (gt_kernels.cu).  All enqueue on `s` and return cudaError_t as int.
+struct LaunchRec;  // profiling hook
+using LaunchHook = void (*)(void* ctx, int kind, bool begin);
+
+enum KernelKind {
+  kKZinvCurl = 0, kKYPass, kKXCross, kKZFwdEpi, kKForce, kKConvert, kKDiag, kKDiagFinal,
+  kKFft1, kKPoint, kNumKinds
+};
+const char* kernel_kind_name(int k);
+
+template <typename R>
+int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
+               void* const out[3], void* const w[6], int mode, void* stream, LaunchHook hook,
+               void* hctx);
+template <typename R>
+int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int n, int serial,
+                 void* stream, LaunchHook hook, void* hctx);
+// Field conversions between the device FP64 staging layout [nz][ny][nhp]
+// double2 and the working precision.
+template <typename R>
+int launch_convert(const Geom& g, const void* src, void* dst, int to_working, void* stream,
+                   LaunchHook hook, void* hctx);
+// Plain 3D transforms of one field (real layout [nz][ny][nx] in w-buffers).
+template <typename R>
+int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real_out,
+                   void* const w[6], void* stream, LaunchHook hook, void* hctx);
+template <typename R>
+int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, void* spec_out,
+                   void* const w[6], void* stream, LaunchHook hook, void* hctx);
+// Pointwise spectral ops used by the output and initial-state paths.
+// op: 0 = curl, 1 = invcurl, 2 = trunc, 3 = incompr (writes |k.a|^2 partials)
+template <typename R>
+int launch_point(const Geom& g, const DevTables<R>& tb, void* const a[3], int op, double* partial,
+                 int npartial, void* stream, LaunchHook hook, void* hctx);
+
+// Diagnostics: per-CTA partials then a fixed-order final reduction.
+constexpr int kDiagScalars = 20;  // 9 energy, 9 enstrophy, helicity, nonfinite
+template <typename R>
+int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const n1[3],
+                double nu, double alpnu, double mu, double alpmu, double* partials, int nblocks,
+                double* result /* kDiagScalars + 3*nbin */, void* stream, LaunchHook hook,
+                void* hctx);
+template <typename R>
+int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], double* partials,
+                  int nblocks, double* result, void* stream, LaunchHook hook, void* hctx);
+int diag_blocks(const Geom& g);
+
+}  // namespace gt

@@ -1,0 +1,997 @@
+// Kernels of the RK2 integrating-factor step and their launchers.
+//
+// One nonlinear-term evaluation nlt(a; bcor) (nlt.f90:16-89) is five passes
+// over HBM, each a batch of 1D FFT lines with the pointwise work fused at
+// the pass boundaries:
+//
+//   1. k_zinv_curl  : per (x-tile, y) column block, u = i k x a and w = k^2 a
+//                     formed on load (produ.f90:44-63, nlt.f90:26-40), then
+//                     the inverse z transform of all six fields.
+//   2. k_spass      : inverse y transform of the six fields, in place.
+//   3. k_xcross     : per pair of (y,z) rows, the six C2R x transforms (two
+//                     fields per complex FFT), u x w in registers
+//                     (produ.f90:9-28), the three R2C x transforms and the
+//                     1/(NX NY NZ) scaling (fft_dir.f90:17-25); real space
+//                     never reaches HBM.
+//   4. k_spass      : forward y transform of the three fields.
+//   5. k_zfwd_epi   : forward z transform, then per mode the Coriolis term
+//                     (nlt.f90:67-81), invcurl (produ.f90:79-101), trunc
+//                     (trunc.f90:10-28) and, in a time step, the
+//                     integrating-factor update step1 (rkstep.f90:30-48) or
+//                     step2 (rkstep.f90:86-104), written straight into the
+//                     stage or state buffers.
+//
+// Spectral fields are [nz][ny][nhp] complex, x fastest, rows padded to a
+// multiple of 128 bytes; columns nh..nhp-1 are never read or written.
+#include <cstdio>
+
+#include "gt_fft.cuh"
+#include "gt_internal.h"
+
+namespace gt {
+
+struct Ptr6 {
+  void* p[6];
+};
+
+constexpr int kSmemBudget = 200 * 1024;
+
+template <typename R> constexpr int max_threads() { return sizeof(R) == 8 ? 512 : 1024; }
+
+static int ilog2i(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: u = curl a, w = k^2 a, inverse z transform of the six fields.
+// Block: (L/8) x TX threads; thread (t, x) owns positions z = t + i L/8 of
+// column X = tile*TX + x.  Shared memory: three [nz][TX] regions.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(max_threads<R>())
+k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int TX = 1 << lgTX;
+  const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
+  const int X = blockIdx.x * TX + x, y = blockIdx.y;
+  const bool valid = X < g.nh;
+  const int lgL = g.lnz, T = g.nz >> 3;
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
+  const int reg = g.nz * TX;
+  C* S0 = sm;
+  C* S1 = sm + reg;
+  C* S2 = sm + 2 * reg;
+  const StridedIdx idx{TX, x};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  const C* a0 = reinterpret_cast<const C*>(a.p[0]);
+  const C* a1 = reinterpret_cast<const C*>(a.p[1]);
+  const C* a2 = reinterpret_cast<const C*>(a.p[2]);
+  const R kx = valid ? tb.fkx[X] : (R)0, ky = tb.fky[y];
+  const R kxs = valid ? tb.fkxs[X] : (R)0, kys = tb.fkys[y];
+  C v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int z = t + i * T;
+    C ux{0, 0}, uy{0, 0}, uz{0, 0};
+    if (valid) {
+      const size_t o = (size_t)z * plane + base;
+      const C ax = a0[o], ay = a1[o], az = a2[o];
+      const R kz = tb.fkz[z];
+      ux = C{-ky * az.y + kz * ay.y, ky * az.x - kz * ay.x};
+      uy = C{-kz * ax.y + kx * az.y, kz * ax.x - kx * az.x};
+      uz = C{-kx * ay.y + ky * ax.y, kx * ay.x - ky * ax.x};
+    }
+    v[i] = ux;
+    S1[idx(z)] = uy;
+    S2[idx(z)] = uz;
+  }
+  C* out0 = reinterpret_cast<C*>(w.p[0]);
+  fft_line<+1, R>(v, t, lgL, tw, S0, idx);
+  if (valid) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out0[(size_t)(t + i * T) * plane + base] = v[i];
+  }
+  for (int f = 1; f < 3; ++f) {
+    C* S = f == 1 ? S1 : S2;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+    __syncthreads();
+    fft_line<+1, R>(v, t, lgL, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.p[f]);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
+    }
+  }
+  for (int c = 0; c < 3; ++c) {
+    const C* ac = reinterpret_cast<const C*>(a.p[c]);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      C val{0, 0};
+      if (valid) {
+        const R k2 = (kxs + kys) + tb.fkzs[z];
+        const C av = ac[(size_t)z * plane + base];
+        val = C{k2 * av.x, k2 * av.y};
+      }
+      v[i] = val;
+    }
+    C* S = c == 0 ? S0 : (c == 1 ? S1 : S2);
+    fft_line<+1, R>(v, t, lgL, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.p[3 + c]);
+    if (valid) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Strided (y or z) transform of up to six fields, in place.  blockIdx.z picks
+// the field, blockIdx.y the outer index (z for a y pass, y for a z pass).
+// ---------------------------------------------------------------------------
+template <typename R, int SIGN>
+__global__ void __launch_bounds__(max_threads<R>())
+k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, int lgTX) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int TX = 1 << lgTX;
+  const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
+  const int X = blockIdx.x * TX + x;
+  const bool valid = X < g.nh;
+  const int T = 1 << (lgL - 3);
+  C* p = reinterpret_cast<C*>(f.p[blockIdx.z]);
+  const size_t base = (size_t)blockIdx.y * (size_t)os + (valid ? X : 0);
+  const StridedIdx idx{TX, x};
+  C v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = valid ? p[base + (size_t)(t + i * T) * (size_t)ls] : C{0, 0};
+  fft_line<SIGN, R>(v, t, lgL, reinterpret_cast<const C*>(twv), sm, idx);
+  if (valid) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) p[base + (size_t)(t + i * T) * (size_t)ls] = v[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3: x transforms with the cross product fused in.  A block holds P
+// pairs of rows; each pair uses three groups of N/8 threads.  Inverse: the
+// half spectra of fields (2q, 2q+1) of one row are packed as X1 + i X2 into
+// one complex line (q = 0..2), so one inverse complex FFT yields both real
+// rows.  Forward: (c_x + i c_y) of row 0, of row 1 and (c_z row 0 + i c_z
+// row 1) are transformed and split with X1 = (Y_k + conj Y_{N-k})/2,
+// X2 = (Y_k - conj Y_{N-k})/(2i).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ Cplx<R> pack_c2r(const Cplx<R>* __restrict__ X1,
+                                            const Cplx<R>* __restrict__ X2, int e, int N) {
+  using C = Cplx<R>;
+  const int h = N >> 1;
+  if (e == 0 || e == h) {  // Re of the DC / Nyquist terms (numpy irfft convention)
+    return C{X1[e].x, X2[e].x};
+  }
+  if (e < h) {
+    const C a = X1[e], b = X2[e];
+    return C{a.x - b.y, a.y + b.x};
+  }
+  const C a = X1[N - e], b = X2[N - e];
+  return C{a.x + b.y, b.x - a.y};
+}
+
+template <typename R>
+__device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R s) {
+  using C = Cplx<R>;
+  return first ? C{(a.x + b.x) * s, (a.y - b.y) * s} : C{(a.y + b.y) * s, (b.x - a.x) * s};
+}
+
+template <typename R>
+__global__ void __launch_bounds__(max_threads<R>())
+k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  const int LP = N + (N >> sh);
+  const int gid = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
+  const int p = gid / 3, q = gid - 3 * p;
+  const size_t pair = (size_t)blockIdx.x * P + p;
+  const C* tw = reinterpret_cast<const C*>(twv);
+  const size_t nhp = g.nhp;
+  C v[8];
+  // inverse: rows 0 and 1 of the pair, field pair q
+  for (int r = 0; r < 2; ++r) {
+    const size_t row = 2 * pair + r;
+    const C* X1 = reinterpret_cast<const C*>(w.p[2 * q]) + row * nhp;
+    const C* X2 = reinterpret_cast<const C*>(w.p[2 * q + 1]) + row * nhp;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N);
+    const PaddedIdx idx{(p * 6 + r * 3 + q) * LP, sh};
+    fft_line<+1, R>(v, t, lgN, tw, sm, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
+  }
+  __syncthreads();
+  // u x w per point of both rows (produ.f90:14-16); u = (z0.x, z0.y, z1.x),
+  // w = (z1.y, z2.x, z2.y) for row 0 and (z3..z5) for row 1.
+  for (int n = threadIdx.x; n < P * N; n += blockDim.x) {
+    const int pp = n >> lgN, e = n & (N - 1);
+    const int o = pp * 6 * LP + e + (e >> sh);
+    const C z0 = sm[o], z1 = sm[o + LP], z2 = sm[o + 2 * LP];
+    const C z3 = sm[o + 3 * LP], z4 = sm[o + 4 * LP], z5 = sm[o + 5 * LP];
+    const R c0x = z0.y * z2.y - z1.x * z2.x;
+    const R c0y = z1.x * z1.y - z0.x * z2.y;
+    const R c0z = z0.x * z2.x - z0.y * z1.y;
+    const R c1x = z3.y * z5.y - z4.x * z5.x;
+    const R c1y = z4.x * z4.y - z3.x * z5.y;
+    const R c1z = z3.x * z5.x - z3.y * z4.y;
+    sm[o] = C{c0x, c0y};
+    sm[o + 3 * LP] = C{c1x, c1y};
+    sm[o + LP] = C{c0z, c1z};
+  }
+  __syncthreads();
+  {
+    const int line = p * 6 + (q == 0 ? 0 : (q == 1 ? 3 : 1));
+    const PaddedIdx idx{line * LP, sh};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
+    __syncthreads();
+    fft_line<-1, R>(v, t, lgN, tw, sm, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
+  }
+  __syncthreads();
+  const int nh = g.nh;
+  const int total = P * 6 * nh;
+  for (int n = threadIdx.x; n < total; n += blockDim.x) {
+    const int k = n % nh;
+    const int rest = n / nh;
+    const int r = rest & 1;
+    const int f = (rest >> 1) % 3;
+    const int pp = (rest >> 1) / 3;
+    const int line = pp * 6 + (f == 2 ? 1 : (r == 0 ? 0 : 3));
+    const bool first = (f == 0) || (f == 2 && r == 0);
+    const int o = line * LP;
+    const int kb = (N - k) & (N - 1);
+    const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
+    const size_t row = 2 * ((size_t)blockIdx.x * P + pp) + r;
+    reinterpret_cast<C*>(w.p[f])[row * nhp + k] = split_r2c<R>(a, b, first, shalf);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 5: forward z transform of three fields, then the spectral epilogue.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(max_threads<R>())
+k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int TX = 1 << lgTX;
+  const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
+  const int X = blockIdx.x * TX + x, y = blockIdx.y;
+  const bool valid = X < g.nh;
+  const int lgL = g.lnz, T = g.nz >> 3;
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
+  const int reg = g.nz * TX;
+  const StridedIdx idx{TX, x};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  C v[8];
+  for (int f = 0; f < 3; ++f) {
+    const C* in = reinterpret_cast<const C*>(w.p[f]);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = valid ? in[(size_t)(t + i * T) * plane + base] : C{0, 0};
+    C* S = sm + f * reg;
+    fft_line<-1, R>(v, t, lgL, tw, S, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+  }
+  if (!valid) return;  // no barrier follows
+  const R kx = tb.fkx[X], ky = tb.fky[y], kxs = tb.fkxs[X], kys = tb.fkys[y];
+  const C* b0p = reinterpret_cast<const C*>(bc.p[0]);
+  const C* b1p = reinterpret_cast<const C*>(bc.p[1]);
+  const C* b2p = reinterpret_cast<const C*>(bc.p[2]);
+  C* o0 = reinterpret_cast<C*>(out.p[0]);
+  C* o1 = reinterpret_cast<C*>(out.p[1]);
+  C* o2 = reinterpret_cast<C*>(out.p[2]);
+  const int* xcut = tb.xcut + (size_t)0;
+#pragma unroll 2
+  for (int i = 0; i < 8; ++i) {
+    const int z = t + i * T;
+    const size_t o = (size_t)z * plane + base;
+    const C n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
+    const C b0 = b0p[o], b1 = b1p[o], b2 = b2p[o];
+    // nlt.f90:67-81: a = v + i omega kz b(t)
+    const R okz = tb.omega * tb.fkz[z];
+    const C a0{n0.x - okz * b0.y, n0.y + okz * b0.x};
+    const C a1{n1.x - okz * b1.y, n1.y + okz * b1.x};
+    const C a2{n2.x - okz * b2.y, n2.y + okz * b2.x};
+    const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
+    const R k2 = (kxs + kys) + tb.fkzs[z];
+    C r0 = a0, r1 = a1, r2 = a2;
+    if (!zero_mode) {  // produ.f90:83-99: i k x a / k^2
+      const R ik2 = (R)1 / k2;
+      const R qx = kx * ik2, qy = ky * ik2, qz = tb.fkz[z] * ik2;
+      r0 = C{-qy * a2.y + qz * a1.y, qy * a2.x - qz * a1.x};
+      r1 = C{-qz * a0.y + qx * a2.y, qz * a0.x - qx * a2.x};
+      r2 = C{-qx * a1.y + qy * a0.y, qx * a1.x - qy * a0.x};
+    }
+    if (tb.truncate && (zero_mode || X >= xcut[(size_t)z * g.ny + y])) {  // trunc.f90:14-28
+      r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
+    }
+    if (mode == kNltOnly) {
+      o0[o] = r0; o1[o] = r1; o2[o] = r2;
+    } else {
+      const R e = tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X];
+      C s0, s1, s2;
+      if (mode == kStage1) {  // rkstep.f90:126-135: c = emk (a + dt2 c)
+        const R d = tb.dt2;
+        s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
+        s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
+        s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};
+      } else {                // rkstep.f90:182-191: a = emk (emk a + dt c)
+        const R d = tb.dt;
+        s0 = C{e * (e * b0.x + d * r0.x), e * (e * b0.y + d * r0.y)};
+        s1 = C{e * (e * b1.x + d * r1.x), e * (e * b1.y + d * r1.y)};
+        s2 = C{e * (e * b2.x + d * r2.x), e * (e * b2.y + d * r2.y)};
+      }
+      if (zero_mode) {        // rkstep.f90:140-144 / 196-200
+        s0 = C{0, 0}; s1 = C{0, 0}; s2 = C{0, 0};
+      }
+      o0[o] = s0; o1[o] = s1; o2[o] = s2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain x transforms (rows of one field packed in pairs).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(max_threads<R>())
+k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, int sh) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  const int LP = N + (N >> sh);
+  const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
+  const size_t pair = (size_t)blockIdx.x * P + p;
+  const C* spec = reinterpret_cast<const C*>(specv);
+  const C* X1 = spec + (2 * pair) * g.nhp;
+  const C* X2 = spec + (2 * pair + 1) * g.nhp;
+  C v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N);
+  fft_line<+1, R>(v, t, lgN, reinterpret_cast<const C*>(twv), sm, PaddedIdx{p * LP, sh});
+  R* r0 = real + (2 * pair) * (size_t)N;
+  R* r1 = real + (2 * pair + 1) * (size_t)N;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    r0[t + i * T] = v[i].x;
+    r1[t + i * T] = v[i].y;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(max_threads<R>())
+k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, int sh, R shalf) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  const int LP = N + (N >> sh);
+  const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
+  const size_t pair = (size_t)blockIdx.x * P + p;
+  const R* r0 = real + (2 * pair) * (size_t)N;
+  const R* r1 = real + (2 * pair + 1) * (size_t)N;
+  C v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = C{r0[t + i * T], r1[t + i * T]};
+  const PaddedIdx idx{p * LP, sh};
+  fft_line<-1, R>(v, t, lgN, reinterpret_cast<const C*>(twv), sm, idx);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
+  __syncthreads();
+  C* spec = reinterpret_cast<C*>(specv);
+  const int nh = g.nh;
+  for (int n = threadIdx.x; n < P * 2 * nh; n += blockDim.x) {
+    const int k = n % nh, rest = n / nh, r = rest & 1, pp = rest >> 1;
+    const int o = pp * LP;
+    const int kb = (N - k) & (N - 1);
+    const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
+    const size_t row = 2 * ((size_t)blockIdx.x * P + pp) + r;
+    spec[row * g.nhp + k] = split_r2c<R>(a, b, r == 0, shalf);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pointwise spectral operators over all modes (output and initial-state
+// paths): 0 curl, 1 invcurl, 2 trunc, 3 incompr (with |k.a|^2 partials).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_point(Ptr6 a, DevTables<R> tb, Geom g, int op, double* partial) {
+  using C = Cplx<R>;
+  __shared__ double red[256];
+  double acc = 0.0;
+  const size_t rows = (size_t)g.ny * g.nz;
+  for (size_t row = blockIdx.y; row < rows; row += gridDim.y) {
+    const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+    for (int X = blockIdx.x * blockDim.x + threadIdx.x; X < g.nh; X += gridDim.x * blockDim.x) {
+      const size_t o = row * g.nhp + X;
+      C* p0 = reinterpret_cast<C*>(a.p[0]);
+      C* p1 = reinterpret_cast<C*>(a.p[1]);
+      C* p2 = reinterpret_cast<C*>(a.p[2]);
+      const C ax = p0[o], ay = p1[o], az = p2[o];
+      const R kx = tb.fkx[X], ky = tb.fky[y], kz = tb.fkz[z];
+      const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
+      const R k2 = (tb.fkxs[X] + tb.fkys[y]) + tb.fkzs[z];
+      if (op == 0) {  // produ.f90:44-63
+        p0[o] = C{-ky * az.y + kz * ay.y, ky * az.x - kz * ay.x};
+        p1[o] = C{-kz * ax.y + kx * az.y, kz * ax.x - kx * az.x};
+        p2[o] = C{-kx * ay.y + ky * ax.y, kx * ay.x - ky * ax.x};
+      } else if (op == 1) {  // produ.f90:79-101
+        if (zero_mode) continue;
+        const R qx = kx / k2, qy = ky / k2, qz = kz / k2;
+        p0[o] = C{-qy * az.y + qz * ay.y, qy * az.x - qz * ay.x};
+        p1[o] = C{-qz * ax.y + qx * az.y, qz * ax.x - qx * az.x};
+        p2[o] = C{-qx * ay.y + qy * ax.y, qx * ay.x - qy * ax.x};
+      } else if (op == 2) {  // trunc.f90:10-28
+        if (zero_mode || X >= tb.xcut[(size_t)z * g.ny + y]) {
+          p0[o] = C{0, 0}; p1[o] = C{0, 0}; p2[o] = C{0, 0};
+        }
+      } else {  // trunc.f90:47-63 with the reduction made explicit
+        if (zero_mode) continue;
+        const C s{kx * ax.x + ky * ay.x + kz * az.x, kx * ax.y + ky * ay.y + kz * az.y};
+        acc += (double)s.x * (double)s.x + (double)s.y * (double)s.y;
+        p0[o] = C{ax.x - s.x * kx / k2, ax.y - s.y * kx / k2};
+        p1[o] = C{ay.x - s.x * ky / k2, ay.y - s.y * ky / k2};
+        p2[o] = C{az.x - s.x * kz / k2, az.y - s.y * kz / k2};
+      }
+    }
+  }
+  if (op == 3) {
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forcing scatter (forcing_3d3c.f90:45-68, forcing_2d2c.f90:37-41): the host
+// drew the increments with the reference RNG; entries are added in order.
+// With no repeated mode in a step the adds commute and run one per thread.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_force(Ptr6 b, const ForceEntry* __restrict__ e, int n, int serial, Geom g) {
+  using C = Cplx<R>;
+  const int first = serial ? 0 : blockIdx.x * blockDim.x + threadIdx.x;
+  const int last = serial ? (threadIdx.x == 0 && blockIdx.x == 0 ? n : 0) : first + 1;
+  for (int m = first; m < last && m < n; ++m) {
+    const ForceEntry en = e[m];
+    const size_t o = ((size_t)en.z * g.ny + en.y) * g.nhp + en.x;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (!(en.mask & (1 << c))) continue;
+      C* p = reinterpret_cast<C*>(b.p[c]);
+      if (sizeof(R) == 8) {
+        const C v = p[o];
+        p[o] = C{(R)((double)v.x + en.inc[2 * c]), (R)((double)v.y + en.inc[2 * c + 1])};
+      } else {
+        const C v = p[o];
+        p[o] = C{v.x + (R)en.inc[2 * c], v.y + (R)en.inc[2 * c + 1]};
+      }
+    }
+  }
+}
+
+template <typename R>
+__global__ void k_convert(const double2* __restrict__ s64, Cplx<R>* __restrict__ w, size_t n,
+                          int to_working) {
+  using C = Cplx<R>;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    if (to_working) {
+      const double2 v = s64[i];
+      w[i] = C{(R)v.x, (R)v.y};
+    } else {
+      const C v = w[i];
+      const_cast<double2*>(s64)[i] = double2{(double)v.x, (double)v.y};
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics.  Each warp walks whole (y,z) rows; along a row |k| grows with
+// kx, so the shell index is non-decreasing and lanes add to warp-private
+// shared bins one lane at a time (fixed order).  Block partials are reduced
+// in block order by k_final_sum: the result is bitwise reproducible.
+// Scalars: [0..8] glob energy terms, [9..17] enstrophy terms, [18] helicity,
+// [19] non-finite count; then E(k) [nbin], E2D(k) [nbin], flux slots [nbin].
+// ---------------------------------------------------------------------------
+constexpr int kDiagThreads = 256;
+
+template <typename R>
+__global__ void __launch_bounds__(kDiagThreads)
+k_diag(Ptr6 bb, Ptr6 nn, DevTables<R> tb, Geom g, double nu, double alpnu, double mu, double alpmu,
+       int has_flux, double* partials, int nq) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* bins = reinterpret_cast<double*>(smraw);  // [8 warps][3][nbin]
+  const int nbin = g.nx / 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < 8 * 3 * nbin; i += blockDim.x) bins[i] = 0.0;
+  __syncthreads();
+  double s[kDiagScalars];
+#pragma unroll
+  for (int q = 0; q < kDiagScalars; ++q) s[q] = 0.0;
+  double* wb = bins + warp * 3 * nbin;
+  const size_t rows = (size_t)g.ny * g.nz;
+  const int nwarps = gridDim.x * 8;
+  for (size_t row = (size_t)blockIdx.x * 8 + warp; row < rows; row += nwarps) {
+    const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+    for (int x0 = 0; x0 < g.nh; x0 += 32) {
+      const int X = x0 + lane;
+      const bool valid = X < g.nh;
+      double vsp = 0.0, v2d = 0.0, vfl = 0.0;
+      int ib = -1;
+      if (valid) {
+        const size_t o = row * g.nhp + X;
+        const C b0 = reinterpret_cast<const C*>(bb.p[0])[o];
+        const C b1 = reinterpret_cast<const C*>(bb.p[1])[o];
+        const C b2 = reinterpret_cast<const C*>(bb.p[2])[o];
+        const double bx0 = b0.x, by0 = b0.y, bx1 = b1.x, by1 = b1.y, bx2 = b2.x, by2 = b2.y;
+        const double kx = tb.fkx[X], ky = tb.fky[y], kz = tb.fkz[z];
+        const double k2 = ((double)tb.fkxs[X] + (double)tb.fkys[y]) + (double)tb.fkzs[z];
+        const double fac = (X == 0 || X == g.nh - 1) ? 0.5 : 1.0;
+        if (!isfinite(bx0) || !isfinite(by0) || !isfinite(bx1) || !isfinite(by1) ||
+            !isfinite(bx2) || !isfinite(by2))
+          s[19] += 1.0;
+        // u = curl b (produ.f90:48-53), w = curl u
+        const double ux0 = -ky * by2 + kz * by1, uy0 = ky * bx2 - kz * bx1;
+        const double ux1 = -kz * by0 + kx * by2, uy1 = kz * bx0 - kx * bx2;
+        const double ux2 = -kx * by1 + ky * by0, uy2 = kx * bx1 - ky * bx0;
+        const double wx0 = -ky * uy2 + kz * uy1, wy0 = ky * ux2 - kz * ux1;
+        const double wx1 = -kz * uy0 + kx * uy2, wy1 = kz * ux0 - kx * ux2;
+        const double wx2 = -kx * uy1 + ky * uy0, wy2 = kx * ux1 - ky * ux0;
+        if (k2 > 0.0) {  // diagnostics.f90:132-145
+          const double pn = alpnu == 1.0 ? k2 : (alpnu == 0.0 ? 1.0 : pow(k2, alpnu));
+          const double pm = alpmu == 1.0 ? k2 : (alpmu == 0.0 ? 1.0 : pow(k2, alpmu));
+          const double e0 = fac * (ux0 * ux0 + uy0 * uy0), e1 = fac * (ux1 * ux1 + uy1 * uy1),
+                       e2 = fac * (ux2 * ux2 + uy2 * uy2);
+          const double z0 = fac * (wx0 * wx0 + wy0 * wy0), z1 = fac * (wx1 * wx1 + wy1 * wy1),
+                       z2 = fac * (wx2 * wx2 + wy2 * wy2);
+          s[0] += e0; s[1] += e1; s[2] += e2;
+          s[3] += 2.0 * nu * e0 * pn; s[4] += 2.0 * nu * e1 * pn; s[5] += 2.0 * nu * e2 * pn;
+          s[6] += 2.0 * mu * e0 * pm; s[7] += 2.0 * mu * e1 * pm; s[8] += 2.0 * mu * e2 * pm;
+          s[9] += z0; s[10] += z1; s[11] += z2;
+          s[12] += 2.0 * nu * z0 * pn; s[13] += 2.0 * nu * z1 * pn; s[14] += 2.0 * nu * z2 * pn;
+          s[15] += 2.0 * mu * z0 * pm; s[16] += 2.0 * mu * z1 * pm; s[17] += 2.0 * mu * z2 * pm;
+          s[18] += fac * (ux0 * wx0 + uy0 * wy0 + ux1 * wx1 + uy1 * wy1 + ux2 * wx2 + uy2 * wy2);
+        }
+        const double kk = sqrt(k2);
+        ib = (int)kk;
+        const double bs = (bx0 * bx0 + by0 * by0) + (bx1 * bx1 + by1 * by1) + (bx2 * bx2 + by2 * by2);
+        vsp = kk * kk * fac * bs;                                 // diagnostics.f90:25-26
+        if (z == 0) v2d = kk * kk * fac * (bx2 * bx2 + by2 * by2);  // :36-40
+        if (has_flux) {                                           // :79-82
+          const C n0 = reinterpret_cast<const C*>(nn.p[0])[o];
+          const C n1 = reinterpret_cast<const C*>(nn.p[1])[o];
+          const C n2 = reinterpret_cast<const C*>(nn.p[2])[o];
+          const double sc = (bx0 * n0.x + by0 * n0.y) + (bx1 * n1.x + by1 * n1.y) +
+                            (bx2 * n2.x + by2 * n2.y);
+          const double f2 = (X == 0 || X == g.nh - 1) ? 1.0 : 2.0;
+          vfl = f2 * kk * kk * sc;
+        }
+      }
+      for (int l = 0; l < 32; ++l) {
+        if (lane == l && ib >= 0) {
+          if (ib + 1 < nbin) {
+            wb[ib] += vsp;
+            if (z == 0) wb[nbin + ib] += v2d;
+          }
+          if (has_flux && ib >= 1 && ib < nbin) wb[2 * nbin + ib] += vfl;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  // block reduction of the scalars: warp shuffle tree, then warps in order
+  __shared__ double wred[8][kDiagScalars];
+#pragma unroll
+  for (int q = 0; q < kDiagScalars; ++q) {
+    double v = s[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) wred[warp][q] = v;
+  }
+  __syncthreads();
+  double* out = partials + (size_t)blockIdx.x * nq;
+  if (threadIdx.x < kDiagScalars) {
+    double v = 0.0;
+    for (int wi = 0; wi < 8; ++wi) v += wred[wi][threadIdx.x];
+    out[threadIdx.x] = v;
+  }
+  for (int i = threadIdx.x; i < 3 * nbin; i += blockDim.x) {
+    double v = 0.0;
+    for (int wi = 0; wi < 8; ++wi) v += bins[wi * 3 * nbin + i];
+    out[kDiagScalars + i] = v;
+  }
+}
+
+// Kinetic energy per component (diagnostics.f90:126-138 energy terms):
+// products in the working precision, accumulation and reduction in FP64.
+template <typename R>
+__global__ void __launch_bounds__(kDiagThreads)
+k_energy(Ptr6 bb, DevTables<R> tb, Geom g, double* partials) {
+  using C = Cplx<R>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+  const size_t rows = (size_t)g.ny * g.nz;
+  const int nwarps = gridDim.x * 8;
+  for (size_t row = (size_t)blockIdx.x * 8 + warp; row < rows; row += nwarps) {
+    const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+    const R ky = tb.fky[y], kz = tb.fkz[z];
+    for (int X = lane; X < g.nh; X += 32) {
+      const size_t o = row * g.nhp + X;
+      const C b0 = reinterpret_cast<const C*>(bb.p[0])[o];
+      const C b1 = reinterpret_cast<const C*>(bb.p[1])[o];
+      const C b2 = reinterpret_cast<const C*>(bb.p[2])[o];
+      const R kx = tb.fkx[X];
+      const R ux0 = -ky * b2.y + kz * b1.y, uy0 = ky * b2.x - kz * b1.x;
+      const R ux1 = -kz * b0.y + kx * b2.y, uy1 = kz * b0.x - kx * b2.x;
+      const R ux2 = -kx * b1.y + ky * b0.y, uy2 = kx * b1.x - ky * b0.x;
+      const double fac = (X == 0 || X == g.nh - 1) ? 0.5 : 1.0;   // k = 0 gives u = 0
+      e0 += fac * (double)(ux0 * ux0 + uy0 * uy0);
+      e1 += fac * (double)(ux1 * ux1 + uy1 * uy1);
+      e2 += fac * (double)(ux2 * ux2 + uy2 * uy2);
+    }
+  }
+  __shared__ double red[8][3];
+  for (int off = 16; off > 0; off >>= 1) {
+    e0 += __shfl_down_sync(0xffffffffu, e0, off);
+    e1 += __shfl_down_sync(0xffffffffu, e1, off);
+    e2 += __shfl_down_sync(0xffffffffu, e2, off);
+  }
+  if (lane == 0) { red[warp][0] = e0; red[warp][1] = e1; red[warp][2] = e2; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double v = 0.0;
+    for (int wi = 0; wi < 8; ++wi) v += red[wi][threadIdx.x];
+    partials[(size_t)blockIdx.x * 3 + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_final_sum(const double* __restrict__ partials, int nblocks, int nq,
+                            double* __restrict__ result) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int b = 0; b < nblocks; ++b) v += partials[(size_t)b * nq + q];
+    result[q] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch configuration.
+// ---------------------------------------------------------------------------
+struct SCfg {
+  int lgTX, threads, smem, ntiles;
+};
+
+static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads) {
+  const int T = L / 8;
+  int TX = 128 / csize;
+  while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
+  int cap = 1;
+  while (cap < nh) cap <<= 1;
+  while (T * TX * 2 <= 256 && TX * 2 <= cap && F * L * TX * 2 * csize <= kSmemBudget &&
+         T * TX * 2 <= maxthreads)
+    TX <<= 1;
+  SCfg c;
+  c.lgTX = ilog2i(TX);
+  c.threads = T * TX;
+  c.smem = F * L * TX * csize;
+  c.ntiles = (nh + TX - 1) / TX;
+  return c;
+}
+
+// Pairs of rows per block for the x passes, and the padding shift.
+static int xpass_pairs(const Geom& g, int groups_per_pair, int csize, int maxthreads,
+                       int lines_per_pair, int sh) {
+  const int T = g.nx / 8;
+  const int LP = g.nx + (g.nx >> sh);
+  const long long npairs = (long long)g.ny * g.nz / 2;
+  int P = 1;
+  while (P * 2 <= npairs && groups_per_pair * T * P * 2 <= maxthreads &&
+         groups_per_pair * T * P * 2 <= 256 && lines_per_pair * LP * P * 2 * csize <= kSmemBudget &&
+         npairs % (P * 2) == 0)
+    P <<= 1;
+  return P;
+}
+
+template <typename R> static int pad_shift() { return sizeof(R) == 8 ? 3 : 4; }
+
+static bool g_attr_done[2] = {false, false};
+
+template <typename R>
+static void set_smem_attrs() {
+  const int idx = sizeof(R) == 8 ? 1 : 0;
+  if (g_attr_done[idx]) return;
+  const int mx = 227 * 1024;
+  cudaFuncSetAttribute(k_zinv_curl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_spass<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_spass<R, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xcross<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_zfwd_epi<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xc2r<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xr2c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_diag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  g_attr_done[idx] = true;
+}
+
+#define GT_HOOK(kind, begin) \
+  if (hook) hook(hctx, (kind), (begin))
+
+template <typename R>
+static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int axis, int sign,
+                 cudaStream_t s, LaunchHook hook, void* hctx) {
+  const int csize = sizeof(Cplx<R>);
+  const int L = axis == 1 ? g.ny : g.nz;
+  const int lgL = axis == 1 ? g.lny : g.lnz;
+  const long long plane = (long long)g.ny * g.nhp;
+  const long long ls = axis == 1 ? g.nhp : plane;
+  const long long os = axis == 1 ? plane : g.nhp;
+  const int outer = axis == 1 ? g.nz : g.ny;
+  SCfg c = strided_cfg(L, g.nh, 1, csize, max_threads<R>());
+  Ptr6 f{};
+  for (int i = 0; i < nf; ++i) f.p[i] = fields[i];
+  dim3 grid(c.ntiles, outer, nf);
+  GT_HOOK(kKYPass, true);
+  if (sign > 0)
+    k_spass<R, 1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX);
+  else
+    k_spass<R, -1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX);
+  GT_HOOK(kKYPass, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
+               void* const out[3], void* const w[6], int mode, void* stream, LaunchHook hook,
+               void* hctx) {
+  set_smem_attrs<R>();
+  cudaStream_t s = (cudaStream_t)stream;
+  const int csize = sizeof(Cplx<R>);
+  int rc;
+  // pass 1
+  {
+    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
+    Ptr6 pa{}, pw{};
+    for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
+    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
+    GT_HOOK(kKZinvCurl, true);
+    k_zinv_curl<R><<<dim3(c.ntiles, g.ny), c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX);
+    GT_HOOK(kKZinvCurl, false);
+    if ((rc = (int)cudaGetLastError())) return rc;
+  }
+  // pass 2
+  if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx))) return rc;
+  // pass 3
+  {
+    const int sh = pad_shift<R>();
+    const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6, sh);
+    const int threads = 3 * P * (g.nx / 8);
+    const int LP = g.nx + (g.nx >> sh);
+    const int smem = 6 * P * LP * csize;
+    const long long nblocks = (long long)g.ny * g.nz / 2 / P;
+    Ptr6 pw{};
+    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
+    const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
+    GT_HOOK(kKXCross, true);
+    k_xcross<R><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf);
+    GT_HOOK(kKXCross, false);
+    if ((rc = (int)cudaGetLastError())) return rc;
+  }
+  // pass 4
+  if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx))) return rc;
+  // pass 5
+  {
+    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
+    Ptr6 pw{}, pb{}, po{};
+    for (int i = 0; i < 3; ++i) {
+      pw.p[i] = w[i];
+      pb.p[i] = bcor[i];
+      po.p[i] = out[i];
+    }
+    GT_HOOK(kKZFwdEpi, true);
+    k_zfwd_epi<R><<<dim3(c.ntiles, g.ny), c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode);
+    GT_HOOK(kKZFwdEpi, false);
+    if ((rc = (int)cudaGetLastError())) return rc;
+  }
+  return 0;
+}
+
+template <typename R>
+int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int n, int serial,
+                 void* stream, LaunchHook hook, void* hctx) {
+  if (n <= 0) return 0;
+  Ptr6 pb{};
+  for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  const int threads = 128;
+  const int blocks = serial ? 1 : (n + threads - 1) / threads;
+  GT_HOOK(kKForce, true);
+  k_force<R><<<blocks, threads, 0, (cudaStream_t)stream>>>(pb, entries, n, serial, g);
+  GT_HOOK(kKForce, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_convert(const Geom& g, const void* src, void* dst, int to_working, void* stream,
+                   LaunchHook hook, void* hctx) {
+  const size_t n = g.field_elems();
+  const int threads = 256;
+  const int blocks = (int)std::min<size_t>((n + threads - 1) / threads, 152 * 16);
+  GT_HOOK(kKConvert, true);
+  if (to_working)
+    k_convert<R><<<blocks, threads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const double2*>(src), reinterpret_cast<Cplx<R>*>(dst), n, 1);
+  else
+    k_convert<R><<<blocks, threads, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const double2*>(dst), reinterpret_cast<Cplx<R>*>(const_cast<void*>(src)),
+        n, 0);
+  GT_HOOK(kKConvert, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real_out,
+                   void* const w[6], void* stream, LaunchHook hook, void* hctx) {
+  set_smem_attrs<R>();
+  cudaStream_t s = (cudaStream_t)stream;
+  (void)w;
+  void* f[1] = {spec};
+  int rc;
+  if ((rc = spass<R>(g, f, 1, tb.twz, 2, +1, s, hook, hctx))) return rc;
+  if ((rc = spass<R>(g, f, 1, tb.twy, 1, +1, s, hook, hctx))) return rc;
+  const int csize = sizeof(Cplx<R>);
+  const int sh = pad_shift<R>();
+  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1, sh);
+  const int LP = g.nx + (g.nx >> sh);
+  const long long nblocks = (long long)g.ny * g.nz / 2 / P;
+  GT_HOOK(kKFft1, true);
+  k_xc2r<R><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(
+      spec, reinterpret_cast<R*>(real_out), g, tb.twx, P, sh);
+  GT_HOOK(kKFft1, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, void* spec_out,
+                   void* const w[6], void* stream, LaunchHook hook, void* hctx) {
+  set_smem_attrs<R>();
+  cudaStream_t s = (cudaStream_t)stream;
+  (void)w;
+  const int csize = sizeof(Cplx<R>);
+  const int sh = pad_shift<R>();
+  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1, sh);
+  const int LP = g.nx + (g.nx >> sh);
+  const long long nblocks = (long long)g.ny * g.nz / 2 / P;
+  const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
+  GT_HOOK(kKFft1, true);
+  k_xr2c<R><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(
+      reinterpret_cast<const R*>(real_in), spec_out, g, tb.twx, P, sh, shalf);
+  GT_HOOK(kKFft1, false);
+  int rc;
+  if ((rc = (int)cudaGetLastError())) return rc;
+  void* f[1] = {spec_out};
+  if ((rc = spass<R>(g, f, 1, tb.twy, 1, -1, s, hook, hctx))) return rc;
+  return spass<R>(g, f, 1, tb.twz, 2, -1, s, hook, hctx);
+}
+
+template <typename R>
+int launch_point(const Geom& g, const DevTables<R>& tb, void* const a[3], int op, double* partial,
+                 int npartial, void* stream, LaunchHook hook, void* hctx) {
+  Ptr6 pa{};
+  for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
+  const int threads = 256;
+  const int bx = (g.nh + threads - 1) / threads;
+  const long long rows = (long long)g.ny * g.nz;
+  int by = (int)std::min<long long>(rows, npartial > 0 ? npartial / bx : 65535);
+  if (by < 1) by = 1;
+  GT_HOOK(kKPoint, true);
+  k_point<R><<<dim3(bx, by), threads, 0, (cudaStream_t)stream>>>(pa, tb, g, op, partial);
+  GT_HOOK(kKPoint, false);
+  int rc = (int)cudaGetLastError();
+  if (rc || op != 3) return rc;
+  GT_HOOK(kKDiagFinal, true);
+  k_final_sum<<<1, 32, 0, (cudaStream_t)stream>>>(partial, bx * by, 1, partial + npartial);
+  GT_HOOK(kKDiagFinal, false);
+  return (int)cudaGetLastError();
+}
+
+int diag_blocks(const Geom& g) {
+  const long long rows = (long long)g.ny * g.nz;
+  long long b = (rows + 7) / 8;
+  return (int)std::min<long long>(b, 152 * 2);
+}
+
+template <typename R>
+int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const n1[3],
+                double nu, double alpnu, double mu, double alpmu, double* partials, int nblocks,
+                double* result, void* stream, LaunchHook hook, void* hctx) {
+  set_smem_attrs<R>();
+  Ptr6 pb{}, pn{};
+  for (int i = 0; i < 3; ++i) {
+    pb.p[i] = b[i];
+    pn.p[i] = n1 ? n1[i] : b[i];
+  }
+  const int nbin = g.nx / 2;
+  const int nq = kDiagScalars + 3 * nbin;
+  const int smem = 8 * 3 * nbin * (int)sizeof(double);
+  GT_HOOK(kKDiag, true);
+  k_diag<R><<<nblocks, kDiagThreads, smem, (cudaStream_t)stream>>>(
+      pb, pn, tb, g, nu, alpnu, mu, alpmu, n1 != nullptr, partials, nq);
+  GT_HOOK(kKDiag, false);
+  int rc = (int)cudaGetLastError();
+  if (rc) return rc;
+  GT_HOOK(kKDiagFinal, true);
+  k_final_sum<<<(nq + 127) / 128, 128, 0, (cudaStream_t)stream>>>(partials, nblocks, nq, result);
+  GT_HOOK(kKDiagFinal, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], double* partials,
+                  int nblocks, double* result, void* stream, LaunchHook hook, void* hctx) {
+  Ptr6 pb{};
+  for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  GT_HOOK(kKDiag, true);
+  k_energy<R><<<nblocks, kDiagThreads, 0, (cudaStream_t)stream>>>(pb, tb, g, partials);
+  GT_HOOK(kKDiag, false);
+  int rc = (int)cudaGetLastError();
+  if (rc) return rc;
+  GT_HOOK(kKDiagFinal, true);
+  k_final_sum<<<1, 32, 0, (cudaStream_t)stream>>>(partials, nblocks, 3, result);
+  GT_HOOK(kKDiagFinal, false);
+  return (int)cudaGetLastError();
+}
+
+const char* kernel_kind_name(int k) {
+  static const char* names[kNumKinds] = {"zinv_curl", "ypass", "xcross", "zfwd_epilogue",
+                                         "force", "convert", "diag", "diag_final",
+                                         "xc2r_xr2c", "pointwise"};
+  return (k >= 0 && k < kNumKinds) ? names[k] : "?";
+}
+
+#define GT_INST(R)                                                                              \
+  template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
+                             void* const*, void* const*, int, void*, LaunchHook, void*);       \
+  template int launch_force<R>(const Geom&, void* const*, const ForceEntry*, int, int, void*,  \
+                               LaunchHook, void*);                                              \
+  template int launch_convert<R>(const Geom&, const void*, void*, int, void*, LaunchHook,      \
+                                 void*);                                                        \
+  template int launch_fft_inv<R>(const Geom&, const DevTables<R>&, void*, void*, void* const*, \
+                                 void*, LaunchHook, void*);                                     \
+  template int launch_fft_dir<R>(const Geom&, const DevTables<R>&, const void*, void*,         \
+                                 void* const*, void*, LaunchHook, void*);                       \
+  template int launch_point<R>(const Geom&, const DevTables<R>&, void* const*, int, double*,   \
+                               int, void*, LaunchHook, void*);                                  \
+  template int launch_energy<R>(const Geom&, const DevTables<R>&, void* const*, double*, int,  \
+                                double*, void*, LaunchHook, void*);                             \
+  template int launch_diag<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,    \
+                              double, double, double, double, double*, int, double*, void*,    \
+                              LaunchHook, void*);
+
+GT_INST(float)
+GT_INST(double)
+
+}  // namespace gt

@@ -1,0 +1,194 @@
+/*
+ * gturbo_gb.h -- C-ABI of the GB300-native RK2 integrating-factor step of
+ * Gturbo3D (triply periodic rotating Navier-Stokes, vector-potential form).
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (GT_OK = 0, a negative GT_E* code otherwise) and never throws.
+ * A handle owns its device memory and one CUDA stream; calls on one handle
+ * must not overlap (a handle is not thread-safe).  Host arrays passed in are
+ * borrowed only for the duration of the call.
+ *
+ * Spectral arrays on the host use the reference layout: complex*16
+ * (NX/2+1, NY, NZ) with x fastest, i.e. double[NZ][NY][NX/2+1][2] in C order
+ * (main.f90:14).  Physical arrays are double[NZ][NY][NX] (the reference's
+ * real*8 (NX+2, NY, NZ) without its two padding columns).
+ *
+ * There is no CPU fallback: compute entry points fail with GT_ECUDA when no
+ * GPU is usable.  The host-only entry points (marked "host only") run
+ * without a GPU.
+ */
+#ifndef GTURBO_GB_H
+#define GTURBO_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GT_OK 0
+#define GT_EINVAL (-1)       /* bad argument or parameter                      */
+#define GT_ENOMEM (-2)       /* device or host allocation failed / over budget */
+#define GT_ECUDA (-3)        /* CUDA runtime error (no device, launch failure) */
+#define GT_ENFORC (-4)       /* more forced modes than NFORC (iniforcing_3d3c.f90:33) */
+#define GT_ENONFINITE (-5)   /* state holds NaN or Inf                         */
+#define GT_EIO (-6)          /* file missing, unreadable or malformed          */
+#define GT_ETIMEOUT (-7)     /* a bounded device wait ran out                  */
+
+/* ---- enumerations ---------------------------------------------------- */
+#define GT_FORCING_NONE 0
+#define GT_FORCING_3D3C 1    /* forcing_3d3c.f90 / iniforcing_3d3c.f90 */
+#define GT_FORCING_2D2C 2    /* forcing_2d2c.f90 / iniforcing_2d2c.f90 */
+
+#define GT_DT2_AS_BUILT 0    /* dt2 = 0: rkstep.f90 reads a dt2 nothing assigns */
+#define GT_DT2_RK2 1         /* dt2 = dt/2: the RK2 midpoint the scheme intends  */
+
+#define GT_PREC_FP64 0       /* plain form: everything in FP64                    */
+#define GT_PREC_MIXED 1      /* FP32 state, FFTs and products; FP64 exponentials,
+                                forcing normalisation and reductions             */
+
+#define GT_NFORC 2048        /* modules.f90:38 */
+
+/* ---- parameters ------------------------------------------------------- */
+/* The values main.f90 reads from params.dat (inieuler.f90:14-20), the
+ * compile-time grid (modules.f90:4, here a runtime value), the link-time
+ * forcing variant (Makefile:20-33) and the choices the reference leaves
+ * implicit. */
+typedef struct gt_params {
+  int32_t nx, ny, nz;          /* powers of two, 8..1024 each                 */
+  double xlx, xly, xlz;        /* box lengths                                 */
+  double nu, alpnu, mu, alpmu; /* hyper-viscosity and friction                */
+  double dt, omega;            /* time step; Coriolis coefficient (nlt.f90:67-81) */
+  double rtrunc;               /* truncation radius, NOT squared (defk.f90:91 squares it) */
+  int32_t truncate;            /* 1: 2/3-rule dealiasing on                   */
+  double famp, k1f, k2f;       /* forcing amplitude and shell k1f < |k| <= k2f */
+  int32_t forcing;             /* GT_FORCING_*                                */
+  int32_t dt2_mode;            /* GT_DT2_*                                    */
+  int32_t precision;           /* GT_PREC_*                                   */
+  int32_t device;              /* CUDA device ordinal                         */
+} gt_params;
+
+/* Global diagnostics (diagnostics.f90:114-199 plus helicity).  energy[] and
+ * enstrophy[] hold, in order: the x, y, z components; the viscous
+ * dissipation 2 nu sum fac |.|^2 k^(2 alpnu) per component; the friction
+ * dissipation per component.  fac = 1/2 on the kx = 0 and kx = NX/2 planes. */
+typedef struct gt_diag {
+  double energy[9];
+  double enstrophy[9];
+  double helicity;             /* sum fac Re(u . conj(w)), k != 0 (no reference counterpart) */
+  double inpe, inpz;           /* mean energy / enstrophy input of the forcing */
+  int64_t nonfinite;           /* number of non-finite state values            */
+} gt_diag;
+
+typedef struct gt_handle gt_handle;
+
+/* ---- host only ---------------------------------------------------------- */
+/* Fills the reference's params.dat defaults for a 2 pi box (params.dat:1-6). */
+int gt_params_default(gt_params* p);
+/* Checks a parameter set (grid sizes, positivity, enum values). */
+int gt_params_validate(const gt_params* p);
+/* Reads params.dat's six list-directed lines (inieuler.f90:14-20) into p;
+ * fields not in the file keep their values.  GT_EIO on a missing or
+ * malformed file. */
+int gt_params_read(const char* path, gt_params* p);
+/* Device bytes gt_create would allocate for p. */
+int gt_memory_estimate(const gt_params* p, size_t* bytes);
+/* One draw of the reference's rann (forcing_3d3c.f90:82-93): advances
+ * *irand and writes REAL*4(irand / (2^31-1)).  n draws in a row. */
+int gt_rann(int32_t* irand, int32_t n, float* out);
+/* Forced-mode list in the reference's order (iniforcing_3d3c.f90:22-184 or
+ * iniforcing_2d2c.f90:14-67).  0-based indices; arrays must hold GT_NFORC
+ * entries (any may be NULL).  GT_ENFORC if the list would exceed GT_NFORC. */
+int gt_forced_modes(const gt_params* p, int32_t* nf, int32_t* ix, int32_t* iy, int32_t* iz,
+                    double* ff, double* inpe, double* inpz);
+/* One step's forcing increments exactly as forcing_3d3c.f90:26-72 or
+ * forcing_2d2c.f90:27-43 compute them, drawn with rann from *seed (which is
+ * advanced).  Writes n entries (mode iz[e], iy[e], ix[e]; dF[e*6 + 2c],
+ * dF[e*6 + 2c + 1] = Re, Im of the increment of component c), in the order
+ * the reference adds them, including the conjugate partners on the kx = 0
+ * and kx = NX/2 planes; cap bounds the arrays (2*GT_NFORC always suffices).
+ * Feed them to gt_rk2_step_coeffs for host-driven forcing. */
+int gt_forcing_increments(const gt_params* p, int32_t* seed, int32_t cap, int32_t* n,
+                          int32_t* ix, int32_t* iy, int32_t* iz, double* dF);
+/* Reads / writes the seed file files/seed.NNN (main.f90:40-45, 207-210). */
+int gt_seed_read(const char* path, int32_t* seed);
+int gt_seed_write(const char* path, int32_t seed);
+/* Reads / writes one float32 real-space field as a Fortran unformatted
+ * sequential record of NX*NY*NZ values, x fastest (read.f90:12-52,
+ * write.f90:12-22). */
+int gt_field_read_f32(const char* path, int32_t nx, int32_t ny, int32_t nz, float* out);
+int gt_field_write_f32(const char* path, int32_t nx, int32_t ny, int32_t nz, const float* in);
+
+/* ---- handle ------------------------------------------------------------- */
+/* Builds the wavenumber tables and integrating factor (defk.f90:13-91), the
+ * forced-mode list (iniforcing_*.f90), the FFT twiddle tables, and
+ * allocates the device state.  The initial state is zero. */
+int gt_create(const gt_params* p, gt_handle** out);
+int gt_destroy(gt_handle* h);
+/* Spectral vector potential b in the host layout described above. */
+int gt_set_state(gt_handle* h, const double* bx, const double* by, const double* bz);
+int gt_get_state(gt_handle* h, double* bx, double* by, double* bz);
+
+/* Drop-in for the body of main.f90:121-150, nsteps times: N1 = nlt(b);
+ * c = step1(b, N1); N2 = nlt(c; Coriolis from b); b = step2(b, N2);
+ * forcing(b, seed).  The forcing draws are made on the host with the
+ * reference's rann, advancing *seed_inout exactly as the reference's
+ * device-resident seed advances.  seed_inout may be NULL when forcing is
+ * GT_FORCING_NONE. */
+int gt_rk2_step(gt_handle* h, int32_t nsteps, int32_t* seed_inout);
+/* One RK2 step with caller-supplied forcing: after step2, adds for each of
+ * n entries the complex increments dF[e*6 + 2c], dF[e*6 + 2c + 1] (component
+ * c = x, y, z) at mode (iz[e], iy[e], ix[e]), in entry order. */
+int gt_rk2_step_coeffs(gt_handle* h, int32_t n, const int32_t* ix, const int32_t* iy,
+                       const int32_t* iz, const double* dF);
+/* Nonlinear term N = nlt(a; Coriolis source = current state) (nlt.f90:1-95)
+ * for a host-supplied a; writes N to the host arrays. */
+int gt_nonlinear(gt_handle* h, const double* ax, const double* ay, const double* az,
+                 double* nx_out, double* ny_out, double* nz_out);
+/* Diagnostics of the current state: glob (diagnostics.f90:114-199),
+ * helicity, spectrum E(k) and E2D(k) (diagnostics.f90:5-56) and the flux
+ * Pi(k) (diagnostics.f90:62-103, evaluated with N1 = nlt(b)).  ek, ek2d and
+ * flux hold NX/2 values each and may be NULL (flux = NULL skips the extra
+ * nlt).  Reductions are FP64 and in a fixed order (bitwise reproducible). */
+int gt_diagnostics(gt_handle* h, gt_diag* out, double* ek, double* ek2d, double* flux);
+/* Kinetic energy of the current state per component, E_c = sum_{k != 0}
+ * fac |(i k x b)_c|^2 (the energy terms of diagnostics.f90:126-138) in FP64,
+ * by a fixed-order reduction: the cheap per-step observable. */
+int gt_energy(gt_handle* h, double* energy_xyz);
+/* 3D transforms of one field through the library's FFT passes:
+ * gt_fft_dir = fft_dir.f90 (R2C scaled by 1/(NX NY NZ)),
+ * gt_fft_inv = fft_inv.f90 (unnormalised C2R). */
+int gt_fft_dir(gt_handle* h, const double* real_in, double* spec_out);
+int gt_fft_inv(gt_handle* h, const double* spec_in, double* real_out);
+/* Velocity u = curl b in physical space (the output path main.f90:188-201). */
+int gt_velocity(gt_handle* h, double* ux, double* uy, double* uz);
+/* Initial-state path (main.f90:91-106): from a physical velocity field, b =
+ * trunc(invcurl(incompr(fft_dir(u)))).  *cc (may be NULL) receives the
+ * removed compressibility sum |k.u|^2 (trunc.f90:47-64). */
+int gt_set_state_physical(gt_handle* h, const double* ux, const double* uy, const double* uz,
+                          double* cc);
+/* GT_ENONFINITE if the state holds a NaN or Inf, GT_OK otherwise. */
+int gt_check_finite(gt_handle* h);
+
+/* ---- introspection ------------------------------------------------------- */
+const char* gt_strerror(int code);
+/* Text of the last CUDA failure seen on the calling thread ("" if none). */
+const char* gt_last_error(void);
+/* The cudaStream_t the handle launches on (for event timing by the caller). */
+int gt_get_stream(gt_handle* h, void** stream);
+/* Number of kernels this handle has launched since creation. */
+int gt_launch_count(gt_handle* h, int64_t* count);
+/* Per-kernel timing: while enabled, each launch is bracketed by CUDA events
+ * on the handle's stream.  gt_profile_read returns, for up to cap kernel
+ * kinds, a name, the number of launches and the summed milliseconds, and
+ * resets the counters. */
+int gt_profile_enable(gt_handle* h, int32_t on);
+int gt_profile_read(gt_handle* h, int32_t cap, char* names /* cap x 32 bytes */,
+                    int64_t* launches, double* ms, int32_t* nkinds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GTURBO_GB_H */

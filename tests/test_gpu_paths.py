@@ -1,0 +1,36 @@
+"""The initial-state path (main.f90:91-106) and the output path
+(main.f90:188-201) against the oracle."""
+import numpy as np
+import pytest
+
+from _helpers import configs, initial, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+def test_velocity_output_path(lib, precision, tol):
+    import gturbo3d_gb300 as g
+    from oracle.gturbo_oracle import Oracle, potential_to_velocity
+    gp, op = configs((32, 16, 32), precision=precision, forcing="none")
+    b = initial((32, 16, 32), seed=4)
+    ref = potential_to_velocity(b, op, Oracle(op).wk)
+    with g.Simulation(gp) as sim:
+        sim.set_state(b)
+        u = sim.velocity()
+    assert relerr(u, ref) < tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+def test_initial_state_path(lib, precision, tol):
+    import gturbo3d_gb300 as g
+    from oracle.gturbo_oracle import Oracle, velocity_to_potential
+    gp, op = configs(32, precision=precision, forcing="none")
+    rng = np.random.default_rng(11)
+    u = [rng.standard_normal((32, 32, 32)) for _ in range(3)]   # compressible noise
+    ref, cc_ref = velocity_to_potential(u, op, Oracle(op).wk)
+    with g.Simulation(gp) as sim:
+        cc = sim.set_state_physical(u)
+        got = sim.get_state()
+    assert relerr(got, ref) < tol
+    assert abs(cc - cc_ref) / cc_ref < max(tol, 1e-12) * 10
