@@ -39,7 +39,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-N = 512
+N = 512           # --size overrides (small cases for profiling only)
 PHYS = dict(nu=2e-4, omega=5.0, dt=1e-3)
 SEED = 2
 INJECTION = 0.1
@@ -48,7 +48,7 @@ UNIT = "steps/s"
 
 
 def workload_config(extra=None):
-    c = {"workload": "rk2_step_512cubed_roofline_config", "grid": [N, N, N], "nu": PHYS["nu"],
+    c = {"workload": f"rk2_step_{N}cubed_roofline_config", "grid": [N, N, N], "nu": PHYS["nu"],
          "omega": PHYS["omega"], "dt": PHYS["dt"], "forcing": "3d3c k in (1.999,3] injection 0.1",
          "seed": SEED, "dt2_mode": "rk2", "truncate": 1,
          "l2_flush": "not needed: 12-field working set (6.6 GB) >> 129 MB L2"}
@@ -312,12 +312,14 @@ def run_ours(args):
     value = ws * args.steps / (ms_max / 1e3)
 
     # --- e2e through the C-ABI with host buffers ------------------------------
-    sim.set_state(b0)
-    e2e_s, _, _ = time_e2e(sim, args.steps, seed, torch)
-    te = torch.tensor([e2e_s], device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = ws * args.steps / float(te.item())
+    e2e_value = None
+    if not args.no_e2e:
+        sim.set_state(b0)
+        e2e_s, _, _ = time_e2e(sim, args.steps, seed, torch)
+        te = torch.tensor([e2e_s], device="cuda")
+        if dist:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e_value = ws * args.steps / float(te.item())
     nf = len(__import__("gturbo3d_gb300").forced_modes(sim.params).ix)
     h2d = (nf + 10) * 64            # ForceEntry records of one step (incl. conjugate partners)
     d2h = 3 * 8                     # three energy components
@@ -327,8 +329,9 @@ def run_ours(args):
     if args.energy_steps > 0 or args.fp64_steps > 0:
         sim64 = make_sim("fp64", device)
         sim64.set_state(b0)
-        ms64, _, prof64, _ = time_steps(sim64, args.fp64_steps, 1, seed, torch, profile=True)
-        fp64_value = args.fp64_steps / (ms64 / 1e3)
+        if args.fp64_steps > 0:
+            ms64, _, prof64, _ = time_steps(sim64, args.fp64_steps, 1, seed, torch, profile=True)
+            fp64_value = args.fp64_steps / (ms64 / 1e3)
         if args.energy_steps > 0:
             sim64.set_state(b0)
             sim64.step(args.energy_steps, seed)
@@ -387,7 +390,11 @@ def main():
     ap.add_argument("--energy-steps", type=int, default=100)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer timing (profiling runs)")
+    ap.add_argument("--size", type=int, default=512, help="grid size (default 512; smaller only for ncu)")
     args = ap.parse_args()
+    global N
+    N = args.size
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -353,6 +353,8 @@ int run_steps(gt_handle* h, int nsteps, const std::vector<ForceEntry>& all,
 
 int set_dev(gt_handle* h) {
   CK(cudaSetDevice(h->p.device));
+  const cudaError_t stale = cudaGetLastError();   // a non-sticky error of an earlier call
+  if (stale != cudaSuccess) g_last_error = std::string("cleared earlier error: ") + cudaGetErrorString(stale);
   return GT_OK;
 }
 

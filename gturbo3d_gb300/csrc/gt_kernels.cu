@@ -720,22 +720,37 @@ static int xpass_pairs(const Geom& g, int groups_per_pair, int csize, int maxthr
 
 template <typename R> static int pad_shift() { return sizeof(R) == 8 ? 3 : 4; }
 
-static bool g_attr_done[2] = {false, false};
+// Opt-in dynamic shared memory: the device's per-block maximum minus the
+// kernel's static shared memory, set once per (device, precision).
+template <typename K>
+static cudaError_t allow_smem(K kernel, int optin) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes);
+}
 
 template <typename R>
-static void set_smem_attrs() {
+static int set_smem_attrs() {
+  static unsigned done_mask[2] = {0u, 0u};   // bit d: device d configured
   const int idx = sizeof(R) == 8 ? 1 : 0;
-  if (g_attr_done[idx]) return;
-  const int mx = 227 * 1024;
-  cudaFuncSetAttribute(k_zinv_curl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_spass<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_spass<R, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xcross<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_zfwd_epi<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xc2r<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xr2c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_diag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  g_attr_done[idx] = true;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 32 && (done_mask[idx] >> dev) & 1u) return 0;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return (int)e;
+  const cudaError_t es[] = {
+      allow_smem(k_zinv_curl<R>, optin), allow_smem(k_spass<R, 1>, optin),
+      allow_smem(k_spass<R, -1>, optin), allow_smem(k_xcross<R>, optin),
+      allow_smem(k_zfwd_epi<R>, optin),  allow_smem(k_xc2r<R>, optin),
+      allow_smem(k_xr2c<R>, optin),      allow_smem(k_diag<R>, optin)};
+  for (cudaError_t x : es)
+    if (x != cudaSuccess) return (int)x;
+  if (dev < 32) done_mask[idx] |= 1u << dev;
+  return 0;
 }
 
 #define GT_HOOK(kind, begin) \
@@ -768,10 +783,10 @@ template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
                void* const out[3], void* const w[6], int mode, void* stream, LaunchHook hook,
                void* hctx) {
-  set_smem_attrs<R>();
+  int rc = set_smem_attrs<R>();
+  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
-  int rc;
   // pass 1
   {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
@@ -855,11 +870,11 @@ int launch_convert(const Geom& g, const void* src, void* dst, int to_working, vo
 template <typename R>
 int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real_out,
                    void* const w[6], void* stream, LaunchHook hook, void* hctx) {
-  set_smem_attrs<R>();
+  int rc = set_smem_attrs<R>();
+  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   (void)w;
   void* f[1] = {spec};
-  int rc;
   if ((rc = spass<R>(g, f, 1, tb.twz, 2, +1, s, hook, hctx))) return rc;
   if ((rc = spass<R>(g, f, 1, tb.twy, 1, +1, s, hook, hctx))) return rc;
   const int csize = sizeof(Cplx<R>);
@@ -877,7 +892,8 @@ int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real
 template <typename R>
 int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, void* spec_out,
                    void* const w[6], void* stream, LaunchHook hook, void* hctx) {
-  set_smem_attrs<R>();
+  int rc = set_smem_attrs<R>();
+  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   (void)w;
   const int csize = sizeof(Cplx<R>);
@@ -890,7 +906,6 @@ int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, v
   k_xr2c<R><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(
       reinterpret_cast<const R*>(real_in), spec_out, g, tb.twx, P, sh, shalf);
   GT_HOOK(kKFft1, false);
-  int rc;
   if ((rc = (int)cudaGetLastError())) return rc;
   void* f[1] = {spec_out};
   if ((rc = spass<R>(g, f, 1, tb.twy, 1, -1, s, hook, hctx))) return rc;
@@ -928,7 +943,8 @@ template <typename R>
 int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const n1[3],
                 double nu, double alpnu, double mu, double alpmu, double* partials, int nblocks,
                 double* result, void* stream, LaunchHook hook, void* hctx) {
-  set_smem_attrs<R>();
+  int rc0 = set_smem_attrs<R>();
+  if (rc0) return rc0;
   Ptr6 pb{}, pn{};
   for (int i = 0; i < 3; ++i) {
     pb.p[i] = b[i];
