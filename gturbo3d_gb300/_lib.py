@@ -76,6 +76,8 @@ SIGNATURES = {
     "gt_velocity": (C.c_int, [_vp, _dp, _dp, _dp]),
     "gt_set_state_physical": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "gt_check_finite": (C.c_int, [_vp]),
+    "gt_set_pruning": (C.c_int, [_vp, C.c_int32]),
+    "gt_pruning_active": (C.c_int, [_vp, _ip]),
     "gt_strerror": (C.c_char_p, [C.c_int]),
     "gt_last_error": (C.c_char_p, []),
     "gt_get_stream": (C.c_int, [_vp, _P(_vp)]),

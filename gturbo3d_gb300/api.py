@@ -255,6 +255,15 @@ class Simulation:
     def check_finite(self) -> int:
         return self.lib.gt_check_finite(self.h)
 
+    def set_pruning(self, enable: bool) -> None:
+        check(self.lib.gt_set_pruning(self.h, 1 if enable else 0), "gt_set_pruning")
+
+    @property
+    def pruning_active(self) -> bool:
+        a = C.c_int32()
+        check(self.lib.gt_pruning_active(self.h, C.byref(a)), "gt_pruning_active")
+        return bool(a.value)
+
     # -- transforms and the initial / output paths ---------------------------
     def fft_dir(self, x):
         x = np.ascontiguousarray(x, np.float64)

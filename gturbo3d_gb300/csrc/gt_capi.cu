@@ -68,6 +68,12 @@ struct gt_handle {
   double* h_result = nullptr;
   int nresult = 0;
   int64_t launches = 0;
+  // truncation-aware pruning: allowed by the caller, the state is zero outside
+  // the kept set K, and every forced mode lies in K
+  bool prune_enabled = true;
+  bool state_in_k = false;
+  bool forcing_in_k = false;
+  unsigned long long* d_count = nullptr;
   bool prof = false;
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> pool;
@@ -174,6 +180,10 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
     return put(c.data(), c.size() * sizeof(R));
   };
   const size_t o_twx = puttw(g.nx), o_twy = puttw(g.ny), o_twz = puttw(g.nz);
+  std::vector<int32_t> tiles;
+  build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles);
+  if (tiles.empty()) tiles = {0, 0};
+  const size_t o_tiles = put(tiles.data(), tiles.size() * sizeof(int32_t));
   (void)nemk;
   void* mem = nullptr;
   CK(cudaMalloc(&mem, buf.size()));
@@ -196,6 +206,9 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   t.dt2 = (R)(h->p.dt2_mode == GT_DT2_RK2 ? 0.5 * h->p.dt : 0.0);
   t.scale = (R)(1.0 / ((double)g.nx * g.ny * g.nz));
   t.truncate = h->p.truncate;
+  t.ztiles = dptr<const int32_t>(mem, o_tiles);
+  t.nztiles = (int)(tiles.size() / 2);
+  t.xa = ht.xcut[0];
   return GT_OK;
 }
 
@@ -218,16 +231,38 @@ void free_handle(gt_handle* h) {
   if (h->tab_mem) cudaFree(h->tab_mem);
   if (h->d_partials) cudaFree(h->d_partials);
   if (h->d_result) cudaFree(h->d_result);
+  if (h->d_count) cudaFree(h->d_count);
   if (h->h_result) cudaFreeHost(h->h_result);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
 
 // ---- dispatch on precision ----------------------------------------------
-int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode) {
+int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
+        int pruned = 0) {
   if (h->mixed)
-    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, h->stream, hook_fn, h);
-  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, h->stream, hook_fn, h);
+    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, h->stream, hook_fn, h);
+  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, pruned, h->stream, hook_fn, h);
+}
+
+bool use_pruning(const gt_handle* h) {
+  return h->prune_enabled && h->p.truncate == 1 && h->state_in_k && h->forcing_in_k;
+}
+
+bool mode_in_k(const gt_handle* h, int z, int y, int x) {
+  return x < h->ht.xcut[(size_t)z * h->g.ny + y];
+}
+
+// Recomputes whether the device state is zero outside K.
+int refresh_state_in_k(gt_handle* h) {
+  int rc = h->mixed ? launch_count_outside<float>(h->g, h->t32, h->b, h->d_count, h->stream)
+                    : launch_count_outside<double>(h->g, h->t64, h->b, h->d_count, h->stream);
+  if (rc) return cuda_fail((cudaError_t)rc, "launch_count_outside");
+  unsigned long long n = 1;
+  CK(cudaMemcpyAsync(&n, h->d_count, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->state_in_k = (n == 0);
+  return GT_OK;
 }
 
 int force(gt_handle* h, const ForceEntry* d, int n, int serial) {
@@ -339,9 +374,10 @@ int run_steps(gt_handle* h, int nsteps, const std::vector<ForceEntry>& all,
     CK(cudaEventRecord(h->force_copied[slot], h->stream));
     dent = h->d_force[slot];
   }
+  const int pr = use_pruning(h) ? 1 : 0;
   for (int s = 0; s < nsteps; ++s) {
-    CKI(nlt(h, h->b, h->b, h->c, kStage1));   // main.f90:124-141
-    CKI(nlt(h, h->c, h->b, h->b, kStage2));   // main.f90:144-146
+    CKI(nlt(h, h->b, h->b, h->c, kStage1, pr));   // main.f90:124-141
+    CKI(nlt(h, h->c, h->b, h->b, kStage2, pr));   // main.f90:144-146
     if (dent) {                               // main.f90:149
       const size_t n = offs[s + 1] - offs[s];
       const bool serial = !entries_unique(all.data() + offs[s], n);
@@ -421,6 +457,13 @@ int gt_create(const gt_params* p, gt_handle** out) {
   CKH(cudaMalloc(&h->d_result, (size_t)h->nresult * sizeof(double)));
   CKH(cudaMallocHost(&h->h_result, (size_t)h->nresult * sizeof(double)));
   for (int i = 0; i < 2; ++i) CKH(cudaEventCreateWithFlags(&h->force_copied[i], cudaEventDisableTiming));
+  CKH(cudaMalloc(&h->d_count, sizeof(unsigned long long)));
+  h->state_in_k = true;   // the zero state
+  h->forcing_in_k = true;
+  for (size_t m = 0; m < h->ht.fix.size(); ++m) {
+    const int x = h->ht.fix[m], y = h->ht.fiy[m], z = h->ht.fiz[m];
+    if (!mode_in_k(h, z, y, x) || !mode_in_k(h, h->ht.kc[z], h->ht.jc[y], x)) h->forcing_in_k = false;
+  }
   CKH(cudaStreamSynchronize(h->stream));
 #undef CKH
   *out = h;
@@ -441,7 +484,7 @@ int gt_set_state(gt_handle* h, const double* bx, const double* by, const double*
   for (int c = 0; c < 3; ++c)
     if ((rc = upload_spec(h, src[c], h->b[c]))) return rc;
   CK(cudaStreamSynchronize(h->stream));
-  return GT_OK;
+  return refresh_state_in_k(h);
 }
 
 int gt_get_state(gt_handle* h, double* bx, double* by, double* bz) {
@@ -491,7 +534,10 @@ int gt_rk2_step_coeffs(gt_handle* h, int32_t n, const int32_t* ix, const int32_t
   int rc = set_dev(h);
   if (rc) return rc;
   std::vector<size_t> offs = {0, all.size()};
-  return run_steps(h, 1, all, offs);
+  rc = run_steps(h, 1, all, offs);
+  for (const ForceEntry& en : all)
+    if (!mode_in_k(h, en.z, en.y, en.x)) h->state_in_k = false;
+  return rc;
 }
 
 int gt_nonlinear(gt_handle* h, const double* ax, const double* ay, const double* az,
@@ -629,7 +675,7 @@ int gt_set_state_physical(gt_handle* h, const double* ux, const double* uy, cons
                      h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (cc) *cc = ccv;
-  return GT_OK;
+  return refresh_state_in_k(h);
 }
 
 int gt_check_finite(gt_handle* h) {
@@ -638,6 +684,18 @@ int gt_check_finite(gt_handle* h) {
   int rc = gt_diagnostics(h, &d, nullptr, nullptr, nullptr);
   if (rc) return rc;
   return d.nonfinite ? GT_ENONFINITE : GT_OK;
+}
+
+int gt_set_pruning(gt_handle* h, int32_t enable) {
+  if (!h) return GT_EINVAL;
+  h->prune_enabled = enable != 0;
+  return GT_OK;
+}
+
+int gt_pruning_active(gt_handle* h, int32_t* active) {
+  if (!h || !active) return GT_EINVAL;
+  *active = use_pruning(h) ? 1 : 0;
+  return GT_OK;
 }
 
 int gt_get_stream(gt_handle* h, void** stream) {

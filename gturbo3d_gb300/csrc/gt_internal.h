@@ -82,6 +82,13 @@ struct DevTables {
   const void* twz;      // nz
   R omega, dt, dt2, scale;  // scale = 1/(nx ny nz)
   int truncate;
+  // Truncation-aware pruning (truncate = 1 and a state that is zero outside
+  // the kept set K): column (X, y) holds nonzero modes only if X < xcut[y]
+  // (the z = 0 row of xcut); ztiles lists the (x-tile, y) blocks of the z
+  // passes that contain such a column; xa = xcut[0] bounds every kept kx.
+  const int32_t* ztiles;   // pairs (x-tile, y)
+  int nztiles;
+  int xa;
 };
 
 enum NltMode { kNltOnly = 0, kStage1 = 1, kStage2 = 2 };
@@ -107,8 +114,14 @@ const char* kernel_kind_name(int k);
 
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, void* stream, LaunchHook hook,
-               void* hctx);
+               void* const out[3], void* const w[6], int mode, int pruned, void* stream,
+               LaunchHook hook, void* hctx);
+// (x-tile, y) blocks of the pruned z passes for precision with complex size csize.
+void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles);
+// Number of state values (over 3 fields) that are nonzero at modes outside K.
+template <typename R>
+int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3],
+                         unsigned long long* d_count, void* stream);
 template <typename R>
 int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int n, int serial,
                  void* stream, LaunchHook hook, void* hctx);

@@ -51,14 +51,19 @@ static int ilog2i(int n) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(max_threads<R>())
-k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX) {
+k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int TX = 1 << lgTX;
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
-  const int X = blockIdx.x * TX + x, y = blockIdx.y;
-  const bool valid = X < g.nh;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tb.ztiles[2 * blockIdx.x];
+    y = tb.ztiles[2 * blockIdx.x + 1];
+  }
+  const int X = tile * TX + x;
+  const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
   const int lgL = g.lnz, T = g.nz >> 3;
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
@@ -78,7 +83,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX) {
   for (int i = 0; i < 8; ++i) {
     const int z = t + i * T;
     C ux{0, 0}, uy{0, 0}, uz{0, 0};
-    if (valid) {
+    if (valid && (!pruned || X < tb.xcut[(size_t)z * g.ny + y])) {
       const size_t o = (size_t)z * plane + base;
       const C ax = a0[o], ay = a1[o], az = a2[o];
       const R kz = tb.fkz[z];
@@ -114,7 +119,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX) {
     for (int i = 0; i < 8; ++i) {
       const int z = t + i * T;
       C val{0, 0};
-      if (valid) {
+      if (valid && (!pruned || X < tb.xcut[(size_t)z * g.ny + y])) {
         const R k2 = (kxs + kys) + tb.fkzs[z];
         const C av = ac[(size_t)z * plane + base];
         val = C{k2 * av.x, k2 * av.y};
@@ -137,25 +142,35 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX) {
 // ---------------------------------------------------------------------------
 template <typename R, int SIGN>
 __global__ void __launch_bounds__(max_threads<R>())
-k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, int lgTX) {
+k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, int lgTX, int xlim,
+        int ymask, const int32_t* __restrict__ xcut0) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int TX = 1 << lgTX;
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
   const int X = blockIdx.x * TX + x;
-  const bool valid = X < g.nh;
+  const bool valid = X < xlim;
   const int T = 1 << (lgL - 3);
   C* p = reinterpret_cast<C*>(f.p[blockIdx.z]);
   const size_t base = (size_t)blockIdx.y * (size_t)os + (valid ? X : 0);
   const StridedIdx idx{TX, x};
   C v[8];
+  // ymask 1 (pruned inverse y pass): only (X, y) with X < xcut0[y] hold data;
+  // ymask 2 (pruned forward y pass): only those are stored.
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = valid ? p[base + (size_t)(t + i * T) * (size_t)ls] : C{0, 0};
+  for (int i = 0; i < 8; ++i) {
+    const int e = t + i * T;
+    const bool ld = valid && (ymask != 1 || X < xcut0[e]);
+    v[i] = ld ? p[base + (size_t)e * (size_t)ls] : C{0, 0};
+  }
   fft_line<SIGN, R>(v, t, lgL, reinterpret_cast<const C*>(twv), sm, idx);
   if (valid) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) p[base + (size_t)(t + i * T) * (size_t)ls] = v[i];
+    for (int i = 0; i < 8; ++i) {
+      const int e = t + i * T;
+      if (ymask != 2 || X < xcut0[e]) p[base + (size_t)e * (size_t)ls] = v[i];
+    }
   }
 }
 
@@ -168,11 +183,14 @@ k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, in
 // row 1) are transformed and split with X1 = (Y_k + conj Y_{N-k})/2,
 // X2 = (Y_k - conj Y_{N-k})/(2i).
 // ---------------------------------------------------------------------------
+// Half-spectrum entries at kx >= xa are zero (pruned pipeline) and are not read.
 template <typename R>
 __device__ __forceinline__ Cplx<R> pack_c2r(const Cplx<R>* __restrict__ X1,
-                                            const Cplx<R>* __restrict__ X2, int e, int N) {
+                                            const Cplx<R>* __restrict__ X2, int e, int N, int xa) {
   using C = Cplx<R>;
   const int h = N >> 1;
+  const int k = e <= h ? e : N - e;
+  if (k >= xa) return C{0, 0};
   if (e == 0 || e == h) {  // Re of the DC / Nyquist terms (numpy irfft convention)
     return C{X1[e].x, X2[e].x};
   }
@@ -192,7 +210,7 @@ __device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R
 
 template <typename R>
 __global__ void __launch_bounds__(max_threads<R>())
-k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf) {
+k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -210,7 +228,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf) {
     const C* X1 = reinterpret_cast<const C*>(w.p[2 * q]) + row * nhp;
     const C* X2 = reinterpret_cast<const C*>(w.p[2 * q + 1]) + row * nhp;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N);
+    for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
     const PaddedIdx idx{(p * 6 + r * 3 + q) * LP, sh};
     fft_line<+1, R>(v, t, lgN, tw, sm, idx);
 #pragma unroll
@@ -246,7 +264,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf) {
     for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
   }
   __syncthreads();
-  const int nh = g.nh;
+  const int nh = xa;   // outputs at kx >= xa are truncated later (pruned) or xa = nh
   const int total = P * 6 * nh;
   for (int n = threadIdx.x; n < total; n += blockDim.x) {
     const int k = n % nh;
@@ -269,14 +287,19 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(max_threads<R>())
-k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode) {
+k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int TX = 1 << lgTX;
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
-  const int X = blockIdx.x * TX + x, y = blockIdx.y;
-  const bool valid = X < g.nh;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tb.ztiles[2 * blockIdx.x];
+    y = tb.ztiles[2 * blockIdx.x + 1];
+  }
+  const int X = tile * TX + x;
+  const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
   const int lgL = g.lnz, T = g.nz >> 3;
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
@@ -305,6 +328,8 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 #pragma unroll 2
   for (int i = 0; i < 8; ++i) {
     const int z = t + i * T;
+    const bool kept = X < xcut[(size_t)z * g.ny + y];
+    if (pruned && !kept) continue;   // zero outside K in both the state and the result
     const size_t o = (size_t)z * plane + base;
     const C n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
     const C b0 = b0p[o], b1 = b1p[o], b2 = b2p[o];
@@ -323,7 +348,7 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
       r1 = C{-qz * a0.y + qx * a2.y, qz * a0.x - qx * a2.x};
       r2 = C{-qx * a1.y + qy * a0.y, qx * a1.x - qy * a0.x};
     }
-    if (tb.truncate && (zero_mode || X >= xcut[(size_t)z * g.ny + y])) {  // trunc.f90:14-28
+    if (tb.truncate && (zero_mode || !kept)) {  // trunc.f90:14-28
       r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
     }
     if (mode == kNltOnly) {
@@ -368,7 +393,7 @@ k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, 
   const C* X2 = spec + (2 * pair + 1) * g.nhp;
   C v[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N);
+  for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, g.nh);
   fft_line<+1, R>(v, t, lgN, reinterpret_cast<const C*>(twv), sm, PaddedIdx{p * LP, sh});
   R* r0 = real + (2 * pair) * (size_t)N;
   R* r1 = real + (2 * pair + 1) * (size_t)N;
@@ -758,7 +783,8 @@ static int set_smem_attrs() {
 
 template <typename R>
 static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int axis, int sign,
-                 cudaStream_t s, LaunchHook hook, void* hctx) {
+                 cudaStream_t s, LaunchHook hook, void* hctx, int xlim = -1, int ymask = 0,
+                 const int32_t* xcut0 = nullptr) {
   const int csize = sizeof(Cplx<R>);
   const int L = axis == 1 ? g.ny : g.nz;
   const int lgL = axis == 1 ? g.lny : g.lnz;
@@ -767,22 +793,24 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
   const long long os = axis == 1 ? plane : g.nhp;
   const int outer = axis == 1 ? g.nz : g.ny;
   SCfg c = strided_cfg(L, g.nh, 1, csize, max_threads<R>());
+  if (xlim < 0) xlim = g.nh;
+  const int TX = 1 << c.lgTX;
   Ptr6 f{};
   for (int i = 0; i < nf; ++i) f.p[i] = fields[i];
-  dim3 grid(c.ntiles, outer, nf);
+  dim3 grid((xlim + TX - 1) / TX, outer, nf);
   GT_HOOK(kKYPass, true);
   if (sign > 0)
-    k_spass<R, 1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX);
+    k_spass<R, 1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
   else
-    k_spass<R, -1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX);
+    k_spass<R, -1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
   GT_HOOK(kKYPass, false);
   return (int)cudaGetLastError();
 }
 
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, void* stream, LaunchHook hook,
-               void* hctx) {
+               void* const out[3], void* const w[6], int mode, int pruned, void* stream,
+               LaunchHook hook, void* hctx) {
   int rc = set_smem_attrs<R>();
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
@@ -793,13 +821,16 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     Ptr6 pa{}, pw{};
     for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
+    const dim3 grid = pruned ? dim3(tb.nztiles) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
-    k_zinv_curl<R><<<dim3(c.ntiles, g.ny), c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX);
+    k_zinv_curl<R><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned);
     GT_HOOK(kKZinvCurl, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
+  const int xlim = pruned ? tb.xa : g.nh;
   // pass 2
-  if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx))) return rc;
+  if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut)))
+    return rc;
   // pass 3
   {
     const int sh = pad_shift<R>();
@@ -812,12 +843,13 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
     GT_HOOK(kKXCross, true);
-    k_xcross<R><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf);
+    k_xcross<R><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf, xlim);
     GT_HOOK(kKXCross, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
   // pass 4
-  if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx))) return rc;
+  if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut)))
+    return rc;
   // pass 5
   {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
@@ -827,8 +859,9 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
       pb.p[i] = bcor[i];
       po.p[i] = out[i];
     }
+    const dim3 grid = pruned ? dim3(tb.nztiles) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZFwdEpi, true);
-    k_zfwd_epi<R><<<dim3(c.ntiles, g.ny), c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode);
+    k_zfwd_epi<R><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned);
     GT_HOOK(kKZFwdEpi, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
@@ -981,6 +1014,48 @@ int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], doubl
   return (int)cudaGetLastError();
 }
 
+void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles) {
+  const SCfg c = strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024);
+  const int TX = 1 << c.lgTX;
+  tiles.clear();
+  for (int y = 0; y < g.ny; ++y)
+    for (int t = 0; t * TX < xcut[y]; ++t) {
+      tiles.push_back(t);
+      tiles.push_back(y);
+    }
+}
+
+template <typename R>
+__global__ void k_count_outside(Ptr6 b, DevTables<R> tb, Geom g, unsigned long long* count) {
+  using C = Cplx<R>;
+  unsigned long long n = 0;
+  const size_t rows = (size_t)g.ny * g.nz;
+  for (size_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int cut = tb.xcut[row];
+    for (int X = cut + threadIdx.x; X < g.nh; X += blockDim.x) {
+      const size_t o = row * g.nhp + X;
+      for (int c = 0; c < 3; ++c) {
+        const C v = reinterpret_cast<const C*>(b.p[c])[o];
+        if (v.x != (R)0 || v.y != (R)0) ++n;
+      }
+    }
+  }
+  if (n) atomicAdd(count, n);
+}
+
+template <typename R>
+int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3],
+                         unsigned long long* d_count, void* stream) {
+  Ptr6 pb{};
+  for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), (cudaStream_t)stream);
+  if (e != cudaSuccess) return (int)e;
+  const long long rows = (long long)g.ny * g.nz;
+  k_count_outside<R><<<(unsigned)std::min<long long>(rows, 152 * 8), 128, 0, (cudaStream_t)stream>>>(
+      pb, tb, g, d_count);
+  return (int)cudaGetLastError();
+}
+
 const char* kernel_kind_name(int k) {
   static const char* names[kNumKinds] = {"zinv_curl", "ypass", "xcross", "zfwd_epilogue",
                                          "force", "convert", "diag", "diag_final",
@@ -990,7 +1065,9 @@ const char* kernel_kind_name(int k) {
 
 #define GT_INST(R)                                                                              \
   template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
-                             void* const*, void* const*, int, void*, LaunchHook, void*);       \
+                             void* const*, void* const*, int, int, void*, LaunchHook, void*);  \
+  template int launch_count_outside<R>(const Geom&, const DevTables<R>&, void* const*,         \
+                                       unsigned long long*, void*);                            \
   template int launch_force<R>(const Geom&, void* const*, const ForceEntry*, int, int, void*,  \
                                LaunchHook, void*);                                              \
   template int launch_convert<R>(const Geom&, const void*, void*, int, void*, LaunchHook,      \

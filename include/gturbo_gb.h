@@ -171,6 +171,15 @@ int gt_set_state_physical(gt_handle* h, const double* ux, const double* uy, cons
                           double* cc);
 /* GT_ENONFINITE if the state holds a NaN or Inf, GT_OK otherwise. */
 int gt_check_finite(gt_handle* h);
+/* Truncation-aware pruning of the time step (on by default).  With
+ * truncate = 1 the state and every nonlinear term live on the kept set K of
+ * trunc.f90:14-17; the step then skips the FFT lines and modes that are zero
+ * and returns the same result up to rounding.  It is used only while the
+ * state is zero outside K (checked on every gt_set_state*, and kept by the
+ * step itself) and every forced mode lies in K. */
+int gt_set_pruning(gt_handle* h, int32_t enable);
+/* *active = 1 if the next gt_rk2_step takes the pruned path. */
+int gt_pruning_active(gt_handle* h, int32_t* active);
 
 /* ---- introspection ------------------------------------------------------- */
 const char* gt_strerror(int code);

@@ -1,0 +1,51 @@
+"""Truncation-aware pruning: the pruned step equals the full step up to
+rounding, and it is used exactly when the state is zero outside K."""
+import numpy as np
+import pytest
+
+from _helpers import configs, initial, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [(32, 32, 32), (64, 32, 16), (16, 64, 32)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-14), ("mixed", 2e-6)])
+def test_pruned_equals_full(lib, n, precision, tol):
+    import gturbo3d_gb300 as g
+    gp, _ = configs(n, precision=precision, forcing="3d3c")
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(n, seed=6)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        b.set_state(b0)
+        b.set_pruning(False)
+        assert a.pruning_active and not b.pruning_active
+        sa = a.step(5, 99)
+        sb = b.step(5, 99)
+        assert sa == sb
+        assert relerr(a.get_state(), b.get_state()) < tol
+        # the pruned state stays exactly zero outside K
+        assert a.pruning_active
+
+
+def test_pruning_follows_the_state(lib):
+    import gturbo3d_gb300 as g
+    gp, _ = configs(32, forcing="3d3c")
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(32, seed=6)
+    with g.Simulation(gp) as sim:
+        assert sim.pruning_active                      # zero state
+        sim.set_state(b0)
+        assert sim.pruning_active
+        bad = [x.copy() for x in b0]
+        bad[0][0, 0, 16] = 1e-3                        # kx = NX/2: outside K
+        sim.set_state(bad)
+        assert not sim.pruning_active
+        sim.step(1, 5)
+        assert not sim.pruning_active
+        sim.set_state(b0)
+        assert sim.pruning_active
+    gp0, _ = configs(32, forcing="3d3c", truncate=0)
+    with g.Simulation(gp0) as sim:
+        sim.set_state(b0)
+        assert not sim.pruning_active                  # no truncation: nothing to prune
