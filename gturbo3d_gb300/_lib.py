@@ -71,6 +71,8 @@ SIGNATURES = {
     "gt_nonlinear": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gt_diagnostics": (C.c_int, [_vp, _P(GtDiag), _dp, _dp, _dp]),
     "gt_energy": (C.c_int, [_vp, _dp]),
+    "gt_energy_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                    C.c_double, C.c_double, _vp, _vp]),
     "gt_fft_dir": (C.c_int, [_vp, _dp, _dp]),
     "gt_fft_inv": (C.c_int, [_vp, _dp, _dp]),
     "gt_velocity": (C.c_int, [_vp, _dp, _dp, _dp]),

@@ -41,6 +41,8 @@ struct Pending {
 
 }  // namespace
 
+void gt::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 struct gt_handle {
   gt_params p{};
   HostTables ht;

@@ -45,6 +45,8 @@ struct ForceEntry {
 };
 
 int build_tables(const gt_params& p, HostTables& t);
+// Records the text gt_last_error() returns on the calling thread.
+void set_last_error(const std::string& msg);
 double emk_value(const gt_params& p, double k2);
 // rann (forcing_3d3c.f90:82-93): advance state, return REAL*4 value.
 float rann(int32_t& irand);

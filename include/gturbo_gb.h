@@ -181,6 +181,26 @@ int gt_set_pruning(gt_handle* h, int32_t enable);
 /* *active = 1 if the next gt_rk2_step takes the pruned path. */
 int gt_pruning_active(gt_handle* h, int32_t* active);
 
+/* Allocation-free kinetic energy, for callers that cannot allocate device
+ * memory: a Fortran driver whose device arrays belong to another runtime (an
+ * OpenACC data region, a pooled allocator holding the HBM) and that must not
+ * call cudaMalloc/cudaFree in its time loop.  This entry point has no
+ * counterpart in the reference.  bx, by, bz are the caller's DEVICE arrays
+ * in the host layout above (FP64, [NZ][NY][NX/2+1][2]); energy_out is a
+ * caller DEVICE array of 3 doubles that receives E_x, E_y, E_z of
+ * gt_energy (same definition, FP64, fixed-order reduction), written on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream).  Scratch is a
+ * fixed 6 MiB array inside the library (one partial per (y,z) row), held by
+ * every GPU that loads the library until the process exits; grids with
+ * NY*NZ > 262144 rows are rejected with GT_EINVAL.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress, with
+ * that device current), so make the first call before any stream capture.
+ * All calls on a device share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+int gt_energy_noalloc(const double* bx, const double* by, const double* bz, int32_t nx,
+                      int32_t ny, int32_t nz, double xlx, double xly, double xlz,
+                      double* energy_out, void* stream);
+
 /* ---- introspection ------------------------------------------------------- */
 const char* gt_strerror(int code);
 /* Text of the last CUDA failure seen on the calling thread ("" if none). */
