@@ -136,6 +136,42 @@ def measured_peaks():
         return None
 
 
+def pass_bytes(n, precision, pruned=True):
+    """Algorithmic bytes per launch of each pass of one nonlinear term: every
+    value a pass must read or write once (no padding, no re-reads).  With the
+    2/3 truncation the pruned passes touch only the active (kx, ky) columns A,
+    the kept set K and kx < xa (the counts follow trunc.f90:14-17)."""
+    import numpy as np
+    nh = n // 2 + 1
+    esz = 8 if precision == "mixed" else 16
+    k = np.arange(n, dtype=float)
+    k = np.where(k > n // 2, k - n, k)
+    kx = np.arange(nh, dtype=float)
+    ks = (n // 2) ** 2
+    rt = 0.6666666666666666667 ** 2
+    tz = (k * k) / ks
+    k1 = (tz[:, None, None] + ((k * k) / ks)[None, :, None]) + ((kx * kx) / ((n // 2) ** 2))[None, None, :]
+    over = k1 > rt
+    xcut = np.where(over.any(axis=2), np.argmax(over, axis=2), nh)
+    if not pruned:
+        xcut[:] = nh
+    A = int(xcut[0].sum())
+    K = int(xcut.sum())
+    xa = int(xcut[0, 0])
+    rows = n * n
+    full = n * n * nh
+    if not pruned:
+        A, K, xa = n * nh, full, nh
+    return {
+        "zinv_curl": (3 * K + 6 * A * n) * esz,
+        "yinv": (6 * A * n + 6 * xa * rows) * esz,
+        "xcross": (9 * xa * rows) * esz,
+        "yfwd": (3 * xa * rows + 3 * A * n) * esz,
+        "zfwd_epilogue": (3 * A * n + 6 * K) * esz,
+        "field_bytes": full * esz,
+    }
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes of each kernel from the committed ncu summary
     (profiles/ncu_traffic.txt: 'kernel precision bytes_per_launch workload')."""
@@ -195,78 +231,67 @@ def time_e2e(sim, steps, seed, torch):
     return dt, np.array(e), s
 
 
-def cpu_baseline(budget_s=30.0):
-    """The FP64 NumPy/SciPy restatement (oracle/) on the host cores: one RK2
-    step on the largest grid of 512/256/128 whose step fits the budget,
-    reported as 512^3-equivalent steps/s by the FFT flop ratio
-    N^3 log2 N^3 (a bounded sample, scaled to the metric's unit)."""
-    import numpy as np
+def _oracle_step_time(n, cores):
+    """Seconds of one FP64 oracle RK2 step (slab-parallel pointwise work,
+    scipy.fft on every core) at n^3, and the sample description."""
     from oracle.gturbo_oracle import Oracle, Params
     from gturbo3d_gb300.synth import initial_potential, forcing_amplitude
-    import scipy.fft as sfft
-    cores = os.cpu_count() or 1
-    est = None
+    p = Params(nx=n, ny=n, nz=n, forcing="3d3c", **PHYS)
+    o = Oracle(p, workers=cores, threads=cores)
+    p.famp = forcing_amplitude(INJECTION, o.fm.nf)
+    o = Oracle(p, workers=cores, threads=cores)
+    b = initial_potential(n, n, n, SEED)
+    t0 = time.perf_counter()
+    o.rk2_step(b, SEED)
+    return time.perf_counter() - t0, o, b
+
+
+def pick_sample_grid(budget_s, cores):
+    """Largest of 64/128/256/512 whose oracle step is predicted (10x per
+    doubling) to fit budget_s; returns (grid, measured step seconds)."""
+    grid, t = 64, _oracle_step_time(64, cores)[0]
     for n in (128, 256, 512):
-        if est is not None and est * 8 * 1.15 > budget_s:
+        if t * 10.0 > budget_s:
             break
-        p = Params(nx=n, ny=n, nz=n, forcing="3d3c", **PHYS)
-        o = Oracle(p, workers=cores)
-        p.famp = forcing_amplitude(INJECTION, o.fm.nf)
-        o = Oracle(p, workers=cores)
-        b = initial_potential(n, n, n, SEED)
-        with sfft.set_workers(cores):
-            t0 = time.perf_counter()
-            o.rk2_step(b, SEED)
-            est = time.perf_counter() - t0
-        grid, t_step = n, est
-        del b, o
+        t_n = _oracle_step_time(n, cores)[0]
+        grid, t = n, t_n
+    return grid, t
+
+
+def cpu_baseline(budget_s=30.0):
+    """The FP64 NumPy/SciPy restatement (oracle/) on the host cores: one RK2
+    step on the largest grid whose step fits the budget, reported as
+    512^3-equivalent steps/s by the FFT flop ratio N^3 log2 N^3 (a bounded
+    sample, scaled to the metric's unit)."""
+    cores = os.cpu_count() or 1
+    grid, t_step = pick_sample_grid(budget_s, cores)
     scale = (N ** 3 * math.log2(N ** 3)) / (grid ** 3 * math.log2(grid ** 3))
     return {"value": 1.0 / (t_step * scale), "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"one FP64 oracle RK2 step at {grid}^3 took {t_step:.2f} s on {cores} threads "
-                      f"(scipy.fft workers={cores}); scaled x{scale:.1f} to 512^3 by N^3 log2 N^3"}
+                      f"(scipy.fft workers={cores}, slab-parallel pointwise); scaled x{scale:.1f} to {N}^3 "
+                      f"by N^3 log2 N^3"}
 
 
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    import scipy.fft as sfft
-    from oracle.gturbo_oracle import Oracle, Params
-    from gturbo3d_gb300.synth import initial_potential, forcing_amplitude
     cores = os.cpu_count() or 1
     budget = 150.0 / max(1, args.steps + args.warmup)
-    # pick the sample grid: largest of 64/128/256/512 whose step fits the per-step budget
-    grid, t_est = 64, None
-    for n in (64, 128, 256, 512):
-        p = Params(nx=n, ny=n, nz=n, forcing="3d3c", **PHYS)
-        o = Oracle(p, workers=cores)
-        p.famp = forcing_amplitude(INJECTION, o.fm.nf)
-        o = Oracle(p, workers=cores)
-        b = initial_potential(n, n, n, SEED)
-        with sfft.set_workers(cores):
-            t0 = time.perf_counter()
-            o.rk2_step(b, SEED)
-            t = time.perf_counter() - t0
-        grid, t_est = n, t
-        if t * 8 * 1.15 > budget:
-            break
-    p = Params(nx=grid, ny=grid, nz=grid, forcing="3d3c", **PHYS)
-    o = Oracle(p, workers=cores)
-    p.famp = forcing_amplitude(INJECTION, o.fm.nf)
-    o = Oracle(p, workers=cores)
-    b = initial_potential(grid, grid, grid, SEED)
+    grid, _ = pick_sample_grid(budget, cores)
+    _, o, b = _oracle_step_time(grid, cores)
     s = SEED
-    with sfft.set_workers(cores):
-        for _ in range(args.warmup):
-            b, s, _ = o.rk2_step(b, s)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            b, s, _ = o.rk2_step(b, s)
-        dt = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b, s, _ = o.rk2_step(b, s)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b, s, _ = o.rk2_step(b, s)
+    dt = time.perf_counter() - t0
     scale = (N ** 3 * math.log2(N ** 3)) / (grid ** 3 * math.log2(grid ** 3))
     value = args.steps / (dt * scale)
-    sample = (f"{args.steps} FP64 oracle RK2 steps at {grid}^3 on {cores} threads took {dt:.2f} s; "
-              f"scaled x{scale:.1f} to 512^3 by N^3 log2 N^3")
+    sample = (f"{args.steps} FP64 oracle RK2 steps at {grid}^3 on {cores} threads took {dt:.2f} s "
+              f"(scipy.fft workers={cores}, slab-parallel pointwise); scaled x{scale:.1f} to {N}^3 "
+              f"by N^3 log2 N^3")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -297,6 +322,7 @@ def run_ours(args):
     # --- mixed form: the headline ---------------------------------------------
     sim = make_sim("mixed", device)
     sim.set_state(b0)
+    pruned = sim.pruning_active
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -344,21 +370,27 @@ def run_ours(args):
     # --- roofline of the dominant kernel --------------------------------------
     peaks = measured_peaks()
     hbm = peaks["hbm_gbs"] if peaks else 6800.0
-    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
-    nh = N // 2 + 1
-    field_bytes = N * N * nh * 8          # one FP32 complex field, algorithmic (no row padding)
+    pbytes = pass_bytes(N, "mixed", pruned=pruned)
+    passes = {k: v for k, v in prof.items() if k in pbytes} if prof else {}
+    dom = max(passes.items(), key=lambda kv: kv[1][1]) if passes else None
     roof = None
     if dom:
         name, (nl, tms) = dom
-        per_launch_bytes = 9 * field_bytes   # every pass moves 9 fields
+        per_launch_bytes = pbytes[name]
         avg_s = tms / nl / 1e3
         achieved = per_launch_bytes / avg_s / 1e9
         traffic = ncu_traffic().get((name, "mixed"))
+        step_bytes = 2 * sum(pbytes[k] for k in ("zinv_curl", "yinv", "xcross", "yfwd", "zfwd_epilogue"))
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3,
-                "kernels": {k: {"launches": v[0], "ms_total": v[1]} for k, v in prof.items()}}
+                "pruned": pruned,
+                "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
+                         "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / hbm},
+                "kernels": {k: {"launches": v[0], "ms_total": v[1],
+                                "gbs": (pbytes[k] * v[0] / (v[1] / 1e3) / 1e9) if k in pbytes else None}
+                            for k, v in prof.items()}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,

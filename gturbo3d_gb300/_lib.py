@@ -80,6 +80,16 @@ SIGNATURES = {
     "gt_check_finite": (C.c_int, [_vp]),
     "gt_set_pruning": (C.c_int, [_vp, C.c_int32]),
     "gt_pruning_active": (C.c_int, [_vp, _ip]),
+    "gt_set_pipelining": (C.c_int, [_vp, C.c_int32]),
+    "gt_set_tuning": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
+    "gt_autotune": (C.c_int, [_vp, C.c_char_p, _dp]),
+    "gt_ensemble_create": (C.c_int, [C.c_int32, _P(GtParams), _P(_vp)]),
+    "gt_ensemble_destroy": (C.c_int, [_vp]),
+    "gt_ensemble_set_state": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
+    "gt_ensemble_get_state": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
+    "gt_ensemble_step": (C.c_int, [_vp, C.c_int32, _ip, C.c_int32]),
+    "gt_ensemble_energy": (C.c_int, [_vp, _dp]),
+    "gt_ensemble_autotune": (C.c_int, [_vp, C.c_char_p]),
     "gt_strerror": (C.c_char_p, [C.c_int]),
     "gt_last_error": (C.c_char_p, []),
     "gt_get_stream": (C.c_int, [_vp, _P(_vp)]),

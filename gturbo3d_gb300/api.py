@@ -255,6 +255,12 @@ class Simulation:
     def check_finite(self) -> int:
         return self.lib.gt_check_finite(self.h)
 
+    def set_pipelining(self, enable: bool) -> None:
+        check(self.lib.gt_set_pipelining(self.h, 1 if enable else 0), "gt_set_pipelining")
+
+    def set_tuning(self, key: str, value: int) -> None:
+        check(self.lib.gt_set_tuning(self.h, key.encode(), int(value)), f"gt_set_tuning({key})")
+
     def set_pruning(self, enable: bool) -> None:
         check(self.lib.gt_set_pruning(self.h, 1 if enable else 0), "gt_set_pruning")
 
@@ -319,3 +325,72 @@ class Simulation:
             nm = raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
             out[nm] = (int(launches[i]), float(ms[i]))
         return out
+
+
+def autotune(sim: "Simulation", cache_path: str | None = None) -> float:
+    """Chooses the fastest launch shapes for sim's grid and precision
+    (gt_autotune); returns the step time in ms, or -1 if taken from the cache."""
+    ms = C.c_double()
+    check(sim.lib.gt_autotune(sim.h, cache_path.encode() if cache_path else None, C.byref(ms)),
+          "gt_autotune")
+    return ms.value
+
+
+class Ensemble:
+    """Independent members advanced together (gt_ensemble_*): in graph mode one
+    captured CUDA graph launch per step advances every member."""
+
+    def __init__(self, params: list):
+        self.lib = load()
+        n = len(params)
+        arr = (GtParams * n)(*params)
+        h = C.c_void_p()
+        check(self.lib.gt_ensemble_create(n, arr, C.byref(h)), "gt_ensemble_create")
+        self.h = h
+        self.n = n
+        self.shapes = [(p.nz, p.ny, p.nx // 2 + 1) for p in params]
+
+    def close(self):
+        if self.h:
+            self.lib.gt_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, i: int, b):
+        b = [np.ascontiguousarray(x, np.complex128) for x in b]
+        if b[0].shape != self.shapes[i]:
+            raise ValueError("shape mismatch")
+        check(self.lib.gt_ensemble_set_state(self.h, i, *(_dp(x.view(np.float64)) for x in b)),
+              "gt_ensemble_set_state")
+
+    def get_state(self, i: int):
+        out = [np.empty(self.shapes[i], np.complex128) for _ in range(3)]
+        check(self.lib.gt_ensemble_get_state(self.h, i, *(_dp(x.view(np.float64)) for x in out)),
+              "gt_ensemble_get_state")
+        return out
+
+    def step(self, nsteps: int, seeds, graph: bool = True) -> np.ndarray:
+        s = np.ascontiguousarray(seeds, np.int32).copy()
+        check(self.lib.gt_ensemble_step(self.h, nsteps, s.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        1 if graph else 0), "gt_ensemble_step")
+        return s
+
+    def energy(self) -> np.ndarray:
+        e = np.zeros(self.n)
+        check(self.lib.gt_ensemble_energy(self.h, _dp(e)), "gt_ensemble_energy")
+        return e
+
+    def autotune(self, cache_path: str | None = None):
+        check(self.lib.gt_ensemble_autotune(self.h, cache_path.encode() if cache_path else None),
+              "gt_ensemble_autotune")

@@ -76,6 +76,11 @@ struct gt_handle {
   bool state_in_k = false;
   bool forcing_in_k = false;
   unsigned long long* d_count = nullptr;
+  // TMA-pipelined y passes (maps of the six work fields) and the device error
+  // flag their bounded waits raise
+  PipeMaps pm{};
+  bool use_pipe = true;
+  int* d_err = nullptr;
   bool prof = false;
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> pool;
@@ -182,10 +187,23 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
     return put(c.data(), c.size() * sizeof(R));
   };
   const size_t o_twx = puttw(g.nx), o_twy = puttw(g.ny), o_twz = puttw(g.nz);
-  std::vector<int32_t> tiles;
+  std::vector<int32_t> tiles, tiles_p;
   build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles);
   if (tiles.empty()) tiles = {0, 0};
   const size_t o_tiles = put(tiles.data(), tiles.size() * sizeof(int32_t));
+  const int ztx = zpipe_tx(g, (int)sizeof(Cplx<R>));
+  build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles_p, ztx > 0 ? ztx : 1);
+  if (tiles_p.empty()) tiles_p = {0, 0};
+  const size_t o_tiles_p = put(tiles_p.data(), tiles_p.size() * sizeof(int32_t));
+  size_t o_tl[5];
+  int n_tl[5];
+  for (int lg = 0; lg < 5; ++lg) {
+    std::vector<int32_t> tl;
+    build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tl, 1 << lg);
+    if (tl.empty()) tl = {0, 0};
+    o_tl[lg] = put(tl.data(), tl.size() * sizeof(int32_t));
+    n_tl[lg] = (int)(tl.size() / 2);
+  }
   (void)nemk;
   void* mem = nullptr;
   CK(cudaMalloc(&mem, buf.size()));
@@ -210,6 +228,12 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   t.truncate = h->p.truncate;
   t.ztiles = dptr<const int32_t>(mem, o_tiles);
   t.nztiles = (int)(tiles.size() / 2);
+  t.ztiles_p = dptr<const int32_t>(mem, o_tiles_p);
+  t.nztiles_p = (int)(tiles_p.size() / 2);
+  for (int lg = 0; lg < 5; ++lg) {
+    t.ztl[lg] = dptr<const int32_t>(mem, o_tl[lg]);
+    t.nztl[lg] = n_tl[lg];
+  }
   t.xa = ht.xcut[0];
   return GT_OK;
 }
@@ -234,6 +258,7 @@ void free_handle(gt_handle* h) {
   if (h->d_partials) cudaFree(h->d_partials);
   if (h->d_result) cudaFree(h->d_result);
   if (h->d_count) cudaFree(h->d_count);
+  if (h->d_err) cudaFree(h->d_err);
   if (h->h_result) cudaFreeHost(h->h_result);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -242,9 +267,25 @@ void free_handle(gt_handle* h) {
 // ---- dispatch on precision ----------------------------------------------
 int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
         int pruned = 0) {
+  const PipeMaps* pm = (h->use_pipe && h->pm.valid) ? &h->pm : nullptr;
   if (h->mixed)
-    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, h->stream, hook_fn, h);
-  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, pruned, h->stream, hook_fn, h);
+    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, pm, h->d_err, h->stream,
+                             hook_fn, h);
+  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, pruned, pm, h->d_err, h->stream,
+                            hook_fn, h);
+}
+
+// Reads (and clears) the device error flag of the bounded waits.
+int check_device_flag(gt_handle* h) {
+  int v = 0;
+  CK(cudaMemcpyAsync(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (v) {
+    CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    g_last_error = "a bounded device wait timed out";
+    return v;
+  }
+  return GT_OK;
 }
 
 bool use_pruning(const gt_handle* h) {
@@ -460,6 +501,9 @@ int gt_create(const gt_params* p, gt_handle** out) {
   CKH(cudaMallocHost(&h->h_result, (size_t)h->nresult * sizeof(double)));
   for (int i = 0; i < 2; ++i) CKH(cudaEventCreateWithFlags(&h->force_copied[i], cudaEventDisableTiming));
   CKH(cudaMalloc(&h->d_count, sizeof(unsigned long long)));
+  CKH(cudaMalloc(&h->d_err, sizeof(int)));
+  CKH(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+  if (make_ypipe_maps(g, h->csize, h->w, h->pm) != 0) h->pm.valid = 0;
   h->state_in_k = true;   // the zero state
   h->forcing_in_k = true;
   for (size_t m = 0; m < h->ht.fix.size(); ++m) {
@@ -498,7 +542,7 @@ int gt_get_state(gt_handle* h, double* bx, double* by, double* bz) {
     if ((rc = download_spec(h, h->b[c], dst[c]))) return rc;
     CK(cudaStreamSynchronize(h->stream));   // the staging buffer is reused
   }
-  return GT_OK;
+  return check_device_flag(h);
 }
 
 int gt_rk2_step(gt_handle* h, int32_t nsteps, int32_t* seed_inout) {
@@ -615,7 +659,7 @@ int gt_energy(gt_handle* h, double* energy_xyz) {
                      h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int c = 0; c < 3; ++c) energy_xyz[c] = h->h_result[c];
-  return GT_OK;
+  return check_device_flag(h);
 }
 
 int gt_fft_dir(gt_handle* h, const double* real_in, double* spec_out) {
@@ -688,6 +732,26 @@ int gt_check_finite(gt_handle* h) {
   return d.nonfinite ? GT_ENONFINITE : GT_OK;
 }
 
+int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
+  if (!h || !key) return GT_EINVAL;
+  const std::string k(key);
+  if (k == "pipe_y") h->pm.pipe_y = value != 0;
+  else if (k == "pipe_z") h->pm.pipe_z = value != 0;
+  else if (k == "pipe_x") h->pm.pipe_x = value != 0;
+  else if (k == "x_pairs" && value >= 1 && value <= 8) h->pm.x_pairs = value;
+  else if (k == "x_stages" && value >= 2 && value <= 4) h->pm.x_stages = value;
+  else if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
+  else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
+  else return GT_EINVAL;
+  return GT_OK;
+}
+
+int gt_set_pipelining(gt_handle* h, int32_t enable) {
+  if (!h) return GT_EINVAL;
+  h->use_pipe = enable != 0;
+  return GT_OK;
+}
+
 int gt_set_pruning(gt_handle* h, int32_t enable) {
   if (!h) return GT_EINVAL;
   h->prune_enabled = enable != 0;
@@ -756,5 +820,419 @@ int gt_profile_read(gt_handle* h, int32_t cap, char* names, int64_t* launches, d
 }
 
 const char* gt_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"
+
+// ===========================================================================
+// Autotuner: coordinate descent over the launch-shape knobs of the pipelined
+// passes, timing whole RK2 steps with CUDA events on a copy of the state;
+// the choice is cached per (grid, precision, pruning, GPU) in a JSON-lines
+// file.
+// ===========================================================================
+namespace {
+
+struct Tuning {
+  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx;
+};
+
+Tuning get_tuning(const gt_handle* h) {
+  return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
+                h->pm.z_tx};
+}
+
+void put_tuning(gt_handle* h, const Tuning& t) {
+  h->pm.pipe_y = t.pipe_y;
+  h->pm.pipe_z = t.pipe_z;
+  h->pm.pipe_x = t.pipe_x;
+  h->pm.x_pairs = t.x_pairs;
+  h->pm.x_stages = t.x_stages;
+  h->pm.y_tx = t.y_tx;
+  h->pm.z_tx = t.z_tx;
+}
+
+std::string tuning_key(const gt_handle* h) {
+  cudaDeviceProp prop;
+  std::string name = "gpu";
+  if (cudaGetDeviceProperties(&prop, h->p.device) == cudaSuccess) name = prop.name;
+  for (char& c : name)
+    if (c == '"' || c == ' ') c = '_';
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%dx%dx%d/%s/%s/%s", h->g.nx, h->g.ny, h->g.nz,
+                h->mixed ? "mixed" : "fp64", use_pruning(h) ? "pruned" : "full", name.c_str());
+  return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  const std::string pat = "\"key\": \"" + key + "\"";
+  while (std::fgets(line, sizeof line, f)) {
+    if (!std::strstr(line, pat.c_str())) continue;
+    Tuning u{};
+    auto get = [&](const char* name, int& v) {
+      const char* q = std::strstr(line, name);
+      return q && std::sscanf(q + std::strlen(name), "%d", &v) == 1;
+    };
+    if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
+        get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
+        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx)) {
+      t = u;
+      found = true;   // the last matching line wins
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void cache_store(const char* path, const std::string& key, const Tuning& t, double ms) {
+  if (!path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f,
+               "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
+               "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"ms_per_step\": %.6f}\n",
+               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, ms);
+  std::fclose(f);
+}
+
+// Mean ms of `steps` RK2 steps (no forcing: the kernels are the same).
+int time_steps(gt_handle* h, int steps, double* ms) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::vector<ForceEntry> none;
+  std::vector<size_t> offs(steps + 1, 0);
+  int rc = run_steps(h, 1, none, offs);   // warm-up (and lazy attribute set-up)
+  if (!rc) {
+    cudaEventRecord(e0, h->stream);
+    rc = run_steps(h, steps, none, offs);
+    cudaEventRecord(e1, h->stream);
+  }
+  if (!rc) {
+    CK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t / steps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
+  const std::string key = tuning_key(h);
+  Tuning t{};
+  if (cache_lookup(cache_path, key, t)) {
+    put_tuning(h, t);
+    if (best_ms_out) *best_ms_out = -1.0;
+    return GT_OK;
+  }
+  // the timing steps overwrite the state: keep a copy
+  const size_t bytes = h->g.field_elems() * h->csize;
+  void* save = nullptr;
+  CK(cudaMalloc(&save, 3 * bytes));
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpyAsync((char*)save + c * bytes, h->b[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
+  const bool was_in_k = h->state_in_k;
+  auto restore = [&]() {
+    for (int c = 0; c < 3; ++c)
+      cudaMemcpyAsync(h->b[c], (char*)save + c * bytes, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    h->state_in_k = was_in_k;
+  };
+  Tuning best = get_tuning(h);
+  double best_ms = 0;
+  int rc = time_steps(h, 3, &best_ms);
+  if (rc) { restore(); cudaFree(save); return rc; }
+  struct Knob { int Tuning::*field; std::vector<int> values; };
+  const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
+                                   {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
+                                   {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
+                                   {&Tuning::x_stages, {2, 3}}};
+  for (const Knob& k : knobs) {
+    for (int v : k.values) {
+      if (best.*(k.field) == v) continue;
+      Tuning cand = best;
+      cand.*(k.field) = v;
+      put_tuning(h, cand);
+      double ms = 0;
+      if (time_steps(h, 3, &ms) == GT_OK && ms < best_ms) {
+        best_ms = ms;
+        best = cand;
+      }
+      cudaGetLastError();   // a shape the device rejects is simply skipped
+    }
+  }
+  put_tuning(h, best);
+  restore();
+  cudaFree(save);
+  cache_store(cache_path, key, best, best_ms);
+  if (best_ms_out) *best_ms_out = best_ms;
+  return GT_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Ensemble: independent members of possibly different grids and parameters,
+// advanced together; in graph mode one CUDA graph launch advances every member
+// by one step (each member's kernels on its own stream, forked and joined in
+// the graph), with the forcing drawn on the host per chunk of steps and read
+// on the device by step index.
+// ===========================================================================
+struct gt_ensemble {
+  std::vector<gt_handle*> m;
+  int device = 0;
+  cudaStream_t master = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool dirty = true;
+  int* d_step = nullptr;
+  std::vector<ForceEntry*> d_ent;
+  std::vector<int> n_ent;
+  int chunk_cap = 0;
+  ForceEntry* h_stage = nullptr;
+  size_t h_cap = 0;
+};
+
+namespace {
+
+constexpr int kEnsembleChunk = 64;
+
+void free_ensemble(gt_ensemble* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->master) cudaStreamSynchronize(e->master);
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  for (auto ev : e->join) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  for (auto p : e->d_ent) if (p) cudaFree(p);
+  if (e->d_step) cudaFree(e->d_step);
+  if (e->h_stage) cudaFreeHost(e->h_stage);
+  for (auto h : e->m) free_handle(h);
+  if (e->master) cudaStreamDestroy(e->master);
+  delete e;
+}
+
+int member_enqueue(gt_ensemble* e, int i) {
+  gt_handle* h = e->m[i];
+  const int pr = use_pruning(h) ? 1 : 0;
+  CKI(nlt(h, h->b, h->b, h->c, kStage1, pr));
+  CKI(nlt(h, h->c, h->b, h->b, kStage2, pr));
+  if (e->n_ent[i] > 0) {
+    if (h->mixed)
+      CKI(launch_force_indexed<float>(h->g, h->b, e->d_ent[i], e->n_ent[i], e->d_step + i, h->stream,
+                                      hook_fn, h));
+    else
+      CKI(launch_force_indexed<double>(h->g, h->b, e->d_ent[i], e->n_ent[i], e->d_step + i, h->stream,
+                                       hook_fn, h));
+  }
+  return GT_OK;
+}
+
+int build_graph(gt_ensemble* e) {
+  if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+  if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+  for (auto h : e->m) h->prof = false;
+  CK(cudaStreamBeginCapture(e->master, cudaStreamCaptureModeRelaxed));
+  int rc = GT_OK;
+  cudaEventRecord(e->fork, e->master);
+  for (size_t i = 0; i < e->m.size() && !rc; ++i) {
+    cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0);
+    rc = member_enqueue(e, (int)i);
+    cudaEventRecord(e->join[i], e->m[i]->stream);
+    cudaStreamWaitEvent(e->master, e->join[i], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(e->master, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+  e->graph = g;
+  CK(cudaGraphInstantiate(&e->exec, e->graph, 0));
+  e->dirty = false;
+  return GT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gt_autotune(gt_handle* h, const char* cache_path, double* best_ms) {
+  if (!h) return GT_EINVAL;
+  int rc = set_dev(h);
+  if (rc) return rc;
+  return autotune_handle(h, cache_path, best_ms);
+}
+
+int gt_ensemble_create(int32_t n, const gt_params* members, gt_ensemble** out) {
+  if (n <= 0 || !members || !out) return GT_EINVAL;
+  *out = nullptr;
+  gt_ensemble* e = new (std::nothrow) gt_ensemble();
+  if (!e) return GT_ENOMEM;
+  e->device = members[0].device;
+  for (int i = 0; i < n; ++i) {
+    if (members[i].device != e->device) { free_ensemble(e); return GT_EINVAL; }
+    gt_handle* h = nullptr;
+    const int rc = gt_create(&members[i], &h);
+    if (rc) { free_ensemble(e); return rc; }
+    e->m.push_back(h);
+  }
+  cudaSetDevice(e->device);
+  cudaError_t ce = cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  e->join.assign(n, nullptr);
+  for (int i = 0; i < n && ce == cudaSuccess; ++i) ce = cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaMalloc(&e->d_step, n * sizeof(int));
+  if (ce != cudaSuccess) { free_ensemble(e); return cuda_fail(ce, "gt_ensemble_create"); }
+  e->n_ent.assign(n, 0);
+  e->d_ent.assign(n, nullptr);
+  // entries per step are fixed by each member's forced-mode list
+  for (int i = 0; i < n; ++i) {
+    gt_handle* h = e->m[i];
+    if (h->p.forcing == GT_FORCING_NONE || h->ht.fix.empty()) continue;
+    std::vector<ForceEntry> one;
+    int32_t seed = 1;
+    draw_forcing(h->p, h->ht, seed, one);
+    e->n_ent[i] = (int)one.size();
+  }
+  *out = e;
+  return GT_OK;
+}
+
+int gt_ensemble_destroy(gt_ensemble* e) {
+  if (!e) return GT_EINVAL;
+  free_ensemble(e);
+  return GT_OK;
+}
+
+int gt_ensemble_set_state(gt_ensemble* e, int32_t i, const double* bx, const double* by, const double* bz) {
+  if (!e || i < 0 || i >= (int)e->m.size()) return GT_EINVAL;
+  e->dirty = true;
+  return gt_set_state(e->m[i], bx, by, bz);
+}
+
+int gt_ensemble_get_state(gt_ensemble* e, int32_t i, double* bx, double* by, double* bz) {
+  if (!e || i < 0 || i >= (int)e->m.size()) return GT_EINVAL;
+  CK(cudaStreamSynchronize(e->master));
+  return gt_get_state(e->m[i], bx, by, bz);
+}
+
+int gt_ensemble_energy(gt_ensemble* e, double* energy) {
+  if (!e || !energy) return GT_EINVAL;
+  CK(cudaStreamSynchronize(e->master));
+  for (size_t i = 0; i < e->m.size(); ++i) {
+    double ex[3];
+    const int rc = gt_energy(e->m[i], ex);
+    if (rc) return rc;
+    energy[i] = ex[0] + ex[1] + ex[2];
+  }
+  return GT_OK;
+}
+
+int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path) {
+  if (!e) return GT_EINVAL;
+  CK(cudaStreamSynchronize(e->master));
+  // one tuning per distinct (grid, precision) class, applied to every member of the class
+  std::vector<std::pair<std::string, Tuning>> done;
+  for (auto h : e->m) {
+    const std::string key = tuning_key(h);
+    bool have = false;
+    for (auto& d : done)
+      if (d.first == key) { put_tuning(h, d.second); have = true; }
+    if (have) continue;
+    const int rc = gt_autotune(h, cache_path, nullptr);
+    if (rc) return rc;
+    done.emplace_back(key, get_tuning(h));
+  }
+  e->dirty = true;
+  return GT_OK;
+}
+
+int gt_ensemble_step(gt_ensemble* e, int32_t nsteps, int32_t* seeds, int32_t graph) {
+  if (!e || nsteps < 0) return GT_EINVAL;
+  const int n = (int)e->m.size();
+  bool forced = false;
+  for (int i = 0; i < n; ++i) forced = forced || e->n_ent[i] > 0;
+  if (forced && !seeds) return GT_EINVAL;
+  CK(cudaSetDevice(e->device));
+  for (auto h : e->m)
+    CK(cudaStreamSynchronize(h->stream));
+  int done = 0;
+  while (done < nsteps) {
+    const int K = std::min(kEnsembleChunk, nsteps - done);
+    // draw and upload K steps of forcing per member
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) total += (size_t)K * e->n_ent[i];
+    CK(cudaStreamSynchronize(e->master));   // the staging buffer is free
+    if (total > e->h_cap) {
+      if (e->h_stage) cudaFreeHost(e->h_stage);
+      e->h_stage = nullptr;
+      e->h_cap = 0;
+      CK(cudaMallocHost(&e->h_stage, total * sizeof(ForceEntry)));
+      e->h_cap = total;
+    }
+    if (K > e->chunk_cap) {
+      for (int i = 0; i < n; ++i) {
+        if (e->d_ent[i]) cudaFree(e->d_ent[i]);
+        e->d_ent[i] = nullptr;
+        if (e->n_ent[i] > 0)
+          CK(cudaMalloc(&e->d_ent[i], (size_t)kEnsembleChunk * e->n_ent[i] * sizeof(ForceEntry)));
+      }
+      e->chunk_cap = kEnsembleChunk;
+      e->dirty = true;   // the entry pointers are baked into the graph
+    }
+    size_t off = 0;
+    for (int i = 0; i < n; ++i) {
+      if (e->n_ent[i] == 0) continue;
+      gt_handle* h = e->m[i];
+      std::vector<ForceEntry> steps;
+      for (int k = 0; k < K; ++k) {
+        const size_t before = steps.size();
+        draw_forcing(h->p, h->ht, seeds[i], steps);
+        if ((int)(steps.size() - before) != e->n_ent[i] ||
+            !entries_unique(steps.data() + before, steps.size() - before))
+          return GT_EINVAL;
+      }
+      std::memcpy(e->h_stage + off, steps.data(), steps.size() * sizeof(ForceEntry));
+      CK(cudaMemcpyAsync(e->d_ent[i], e->h_stage + off, steps.size() * sizeof(ForceEntry),
+                         cudaMemcpyHostToDevice, e->master));
+      off += steps.size();
+    }
+    CK(cudaMemsetAsync(e->d_step, 0, n * sizeof(int), e->master));
+    if (graph) {
+      if (e->dirty) {
+        const int rc = build_graph(e);
+        if (rc) return rc;
+      }
+      for (int k = 0; k < K; ++k) CK(cudaGraphLaunch(e->exec, e->master));
+    } else {
+      // one launch sequence per member and step, each member on its own stream
+      CK(cudaEventRecord(e->fork, e->master));
+      for (int i = 0; i < n; ++i) CK(cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0));
+      for (int k = 0; k < K; ++k)
+        for (int i = 0; i < n; ++i) {
+          const int rc = member_enqueue(e, i);
+          if (rc) return rc;
+        }
+      for (int i = 0; i < n; ++i) {
+        CK(cudaEventRecord(e->join[i], e->m[i]->stream));
+        CK(cudaStreamWaitEvent(e->master, e->join[i], 0));
+      }
+    }
+    done += K;
+  }
+  CK(cudaStreamSynchronize(e->master));
+  for (auto h : e->m) {
+    const int rc = check_device_flag(h);
+    if (rc) return rc;
+  }
+  return GT_OK;
+}
 
 }  // extern "C"

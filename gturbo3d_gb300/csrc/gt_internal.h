@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/gturbo_gb.h"
 
 namespace gt {
@@ -88,12 +90,34 @@ struct DevTables {
   // the kept set K): column (X, y) holds nonzero modes only if X < xcut[y]
   // (the z = 0 row of xcut); ztiles lists the (x-tile, y) blocks of the z
   // passes that contain such a column; xa = xcut[0] bounds every kept kx.
-  const int32_t* ztiles;   // pairs (x-tile, y)
+  const int32_t* ztiles;   // pairs (x-tile, y) for the default z tile width
   int nztiles;
+  const int32_t* ztiles_p; // the same for the tile width of the pipelined z pass
+  int nztiles_p;
+  const int32_t* ztl[5];   // the same for tile widths 1, 2, 4, 8, 16 (tuning)
+  int nztl[5];
   int xa;
 };
 
 enum NltMode { kNltOnly = 0, kStage1 = 1, kStage2 = 2 };
+
+// TMA tensor maps of the six work fields for the pipelined y passes
+// (box: 2*ytx scalars x 16 rows x 1 plane).
+struct PipeMaps {
+  CUtensorMap y[6];   // y passes: box 2*ytx x 16 rows x 1 plane, fields w[0..5]
+  CUtensorMap z[3];   // z forward pass: box 2*ztx x 1 row x min(nz,256) planes, w[0..2]
+  int ytx, ztx;
+  int valid;
+  // tuning: 0 = one-tile-per-CTA pass, 1 = pipelined (per pass)
+  int pipe_y = 0, pipe_z = 0, pipe_x = 0;
+  int x_pairs = 1, x_stages = 2;
+  int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
+};
+using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                     const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                     const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                     CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+PFN_encodeTiled get_encode_tiled();
 
 // Work buffers: w[0..5] hold u_x,u_y,u_z,w_x,w_y,w_z between passes; after
 // the x-pass w[0..2] hold u x w.
@@ -110,16 +134,33 @@ using LaunchHook = void (*)(void* ctx, int kind, bool begin);
 
 enum KernelKind {
   kKZinvCurl = 0, kKYPass, kKXCross, kKZFwdEpi, kKForce, kKConvert, kKDiag, kKDiagFinal,
-  kKFft1, kKPoint, kNumKinds
+  kKFft1, kKPoint, kKYFwd, kNumKinds
 };
 const char* kernel_kind_name(int k);
 
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, int pruned, void* stream,
-               LaunchHook hook, void* hctx);
+               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+               int* err, void* stream, LaunchHook hook, void* hctx);
+// Default tile width of the plain z passes (3 fields in shared memory).
+int zpass_default_tx(const Geom& g, int csize);
+int ypipe_tx(const Geom& g, int csize);
+int zpipe_tx(const Geom& g, int csize);
+template <typename R>
+int launch_xpipe(const Geom& g, void* const w[6], const void* twx, int xa, int pairs, int nstage,
+                 int* err, void* stream, LaunchHook hook, void* hctx);
+template <typename R>
+int launch_zpipe_epi(const Geom& g, const DevTables<R>& tb, const PipeMaps& pm, void* const bcor[3],
+                     void* const out[3], int mode, int pruned, int* err, void* stream, LaunchHook hook,
+                     void* hctx);
+int make_ypipe_maps(const Geom& g, int csize, void* const w[6], PipeMaps& pm);
+template <typename R>
+int launch_ypipe(const Geom& g, const PipeMaps& pm, void* const* fields, int nf, const void* tw,
+                 int sign, int xlim, int ymask, const int32_t* xcut0, int* err, void* stream,
+                 LaunchHook hook, void* hctx);
 // (x-tile, y) blocks of the pruned z passes for precision with complex size csize.
-void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles);
+void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles,
+                  int tx = 0);
 // Number of state values (over 3 fields) that are nonzero at modes outside K.
 template <typename R>
 int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3],
@@ -127,6 +168,10 @@ int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3]
 template <typename R>
 int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int n, int serial,
                  void* stream, LaunchHook hook, void* hctx);
+// Forcing of step *step from resident per-step entries, then ++*step.
+template <typename R>
+int launch_force_indexed(const Geom& g, void* const b[3], const ForceEntry* base, int n,
+                         const int* step, void* stream, LaunchHook hook, void* hctx);
 // Field conversions between the device FP64 staging layout [nz][ny][nhp]
 // double2 and the working precision.
 template <typename R>

@@ -51,7 +51,7 @@ static int ilog2i(int n) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(max_threads<R>())
-k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned) {
+k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -59,8 +59,8 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned) {
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
   int tile = blockIdx.x, y = blockIdx.y;
   if (pruned) {
-    tile = tb.ztiles[2 * blockIdx.x];
-    y = tb.ztiles[2 * blockIdx.x + 1];
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
   }
   const int X = tile * TX + x;
   const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
@@ -184,22 +184,23 @@ k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, in
 // X2 = (Y_k - conj Y_{N-k})/(2i).
 // ---------------------------------------------------------------------------
 // Half-spectrum entries at kx >= xa are zero (pruned pipeline) and are not read.
+// Z_e = X1_e + i X2_e (e < N/2), conj(X1_{N-e}) + i conj(X2_{N-e}) (e > N/2);
+// at e = 0 and N/2 only the real parts enter (numpy irfft convention).
 template <typename R>
 __device__ __forceinline__ Cplx<R> pack_c2r(const Cplx<R>* __restrict__ X1,
                                             const Cplx<R>* __restrict__ X2, int e, int N, int xa) {
   using C = Cplx<R>;
   const int h = N >> 1;
-  const int k = e <= h ? e : N - e;
+  const bool hi = e > h;
+  const int k = hi ? N - e : e;
   if (k >= xa) return C{0, 0};
-  if (e == 0 || e == h) {  // Re of the DC / Nyquist terms (numpy irfft convention)
-    return C{X1[e].x, X2[e].x};
+  C a = X1[k], b = X2[k];
+  if (k == 0 || k == h) {
+    a.y = 0;
+    b.y = 0;
   }
-  if (e < h) {
-    const C a = X1[e], b = X2[e];
-    return C{a.x - b.y, a.y + b.x};
-  }
-  const C a = X1[N - e], b = X2[N - e];
-  return C{a.x + b.y, b.x - a.y};
+  const R sg = hi ? (R)-1 : (R)1;
+  return C{a.x - sg * b.y, sg * a.y + b.x};
 }
 
 template <typename R>
@@ -264,21 +265,22 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
     for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
   }
   __syncthreads();
-  const int nh = xa;   // outputs at kx >= xa are truncated later (pruned) or xa = nh
-  const int total = P * 6 * nh;
-  for (int n = threadIdx.x; n < total; n += blockDim.x) {
-    const int k = n % nh;
-    const int rest = n / nh;
-    const int r = rest & 1;
-    const int f = (rest >> 1) % 3;
-    const int pp = (rest >> 1) / 3;
-    const int line = pp * 6 + (f == 2 ? 1 : (r == 0 ? 0 : 3));
-    const bool first = (f == 0) || (f == 2 && r == 0);
-    const int o = line * LP;
-    const int kb = (N - k) & (N - 1);
-    const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
-    const size_t row = 2 * ((size_t)blockIdx.x * P + pp) + r;
-    reinterpret_cast<C*>(w.p[f])[row * nhp + k] = split_r2c<R>(a, b, first, shalf);
+  // Group q of pair p writes field q (c_x, c_y, c_z) of both rows; kx >= xa
+  // is truncated later (pruned) or xa = nh.
+  {
+    const int lineA = p * 6 + (q == 2 ? 1 : 0), lineB = p * 6 + (q == 2 ? 1 : 3);
+    C* out = reinterpret_cast<C*>(w.p[q]);
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int o = (r == 0 ? lineA : lineB) * LP;
+      const bool first = (q == 0) || (q == 2 && r == 0);
+      C* orow = out + (2 * pair + r) * nhp;
+      for (int k = t; k < xa; k += T) {
+        const int kb = (N - k) & (N - 1);
+        const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
+        orow[k] = split_r2c<R>(a, b, first, shalf);
+      }
+    }
   }
 }
 
@@ -287,7 +289,8 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(max_threads<R>())
-k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned) {
+k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
+           const int32_t* __restrict__ tiles) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -295,8 +298,8 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
   int tile = blockIdx.x, y = blockIdx.y;
   if (pruned) {
-    tile = tb.ztiles[2 * blockIdx.x];
-    y = tb.ztiles[2 * blockIdx.x + 1];
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
   }
   const int X = tile * TX + x;
   const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
@@ -520,6 +523,33 @@ __global__ void k_force(Ptr6 b, const ForceEntry* __restrict__ e, int n, int ser
   }
 }
 
+// Graph-replayable forcing: the entries of every step of a chunk are resident
+// ([step][n] in `base`); a device counter selects the step, and k_step_inc
+// advances it after the scatter, so one captured graph serves every step.
+template <typename R>
+__global__ void k_force_indexed(Ptr6 b, const ForceEntry* __restrict__ base, int n,
+                                const int* __restrict__ step, Geom g) {
+  using C = Cplx<R>;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const ForceEntry en = base[(size_t)(*step) * n + m];
+  const size_t o = ((size_t)en.z * g.ny + en.y) * g.nhp + en.x;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (!(en.mask & (1 << c))) continue;
+    C* p = reinterpret_cast<C*>(b.p[c]);
+    const C v = p[o];
+    if (sizeof(R) == 8)
+      p[o] = C{(R)((double)v.x + en.inc[2 * c]), (R)((double)v.y + en.inc[2 * c + 1])};
+    else
+      p[o] = C{v.x + (R)en.inc[2 * c], v.y + (R)en.inc[2 * c + 1]};
+  }
+}
+
+__global__ void k_step_inc(int* step) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
+}
+
 template <typename R>
 __global__ void k_convert(const double2* __restrict__ s64, Cplx<R>* __restrict__ w, size_t n,
                           int to_working) {
@@ -712,8 +742,18 @@ struct SCfg {
   int lgTX, threads, smem, ntiles;
 };
 
-static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads) {
+static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads, int force_tx = 0) {
   const int T = L / 8;
+  if (force_tx > 0) {
+    int TX = force_tx;
+    while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
+    SCfg c;
+    c.lgTX = ilog2i(TX);
+    c.threads = T * TX;
+    c.smem = F * L * TX * csize;
+    c.ntiles = (nh + TX - 1) / TX;
+    return c;
+  }
   int TX = 128 / csize;
   while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
   int cap = 1;
@@ -784,7 +824,7 @@ static int set_smem_attrs() {
 template <typename R>
 static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int axis, int sign,
                  cudaStream_t s, LaunchHook hook, void* hctx, int xlim = -1, int ymask = 0,
-                 const int32_t* xcut0 = nullptr) {
+                 const int32_t* xcut0 = nullptr, int force_tx = 0) {
   const int csize = sizeof(Cplx<R>);
   const int L = axis == 1 ? g.ny : g.nz;
   const int lgL = axis == 1 ? g.lny : g.lnz;
@@ -792,47 +832,58 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
   const long long ls = axis == 1 ? g.nhp : plane;
   const long long os = axis == 1 ? plane : g.nhp;
   const int outer = axis == 1 ? g.nz : g.ny;
-  SCfg c = strided_cfg(L, g.nh, 1, csize, max_threads<R>());
+  SCfg c = strided_cfg(L, g.nh, 1, csize, max_threads<R>(), force_tx);
   if (xlim < 0) xlim = g.nh;
   const int TX = 1 << c.lgTX;
   Ptr6 f{};
   for (int i = 0; i < nf; ++i) f.p[i] = fields[i];
   dim3 grid((xlim + TX - 1) / TX, outer, nf);
-  GT_HOOK(kKYPass, true);
+  const int kind = sign > 0 ? kKYPass : kKYFwd;
+  GT_HOOK(kind, true);
   if (sign > 0)
     k_spass<R, 1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
   else
     k_spass<R, -1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
-  GT_HOOK(kKYPass, false);
+  GT_HOOK(kind, false);
   return (int)cudaGetLastError();
 }
 
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, int pruned, void* stream,
-               LaunchHook hook, void* hctx) {
+               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+               int* err, void* stream, LaunchHook hook, void* hctx) {
   int rc = set_smem_attrs<R>();
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
+  const int ztx = pm ? pm->z_tx : 0;
   // pass 1
   {
-    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
+    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
     Ptr6 pa{}, pw{};
     for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
-    const dim3 grid = pruned ? dim3(tb.nztiles) : dim3(c.ntiles, g.ny);
+    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
-    k_zinv_curl<R><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned);
+    k_zinv_curl<R><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
     GT_HOOK(kKZinvCurl, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
   const int xlim = pruned ? tb.xa : g.nh;
   // pass 2
-  if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut)))
+  if (pm && pm->valid && pm->pipe_y) {
+    if ((rc = launch_ypipe<R>(g, *pm, w, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
+                              hook, hctx)))
+      return rc;
+  } else if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
+                            pm ? pm->y_tx : 0))) {
     return rc;
+  }
   // pass 3
-  {
+  if (pm && pm->valid && pm->pipe_x) {
+    if ((rc = launch_xpipe<R>(g, w, tb.twx, xlim, pm->x_pairs, pm->x_stages, err, stream, hook, hctx)))
+      return rc;
+  } else {
     const int sh = pad_shift<R>();
     const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6, sh);
     const int threads = 3 * P * (g.nx / 8);
@@ -848,20 +899,29 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     if ((rc = (int)cudaGetLastError())) return rc;
   }
   // pass 4
-  if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut)))
+  if (pm && pm->valid && pm->pipe_y) {
+    if ((rc = launch_ypipe<R>(g, *pm, w, 3, tb.twy, -1, xlim, pruned ? 2 : 0, tb.xcut, err, stream,
+                              hook, hctx)))
+      return rc;
+  } else if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
+                            pm ? pm->y_tx : 0))) {
     return rc;
+  }
   // pass 5
-  {
-    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>());
+  if (pm && pm->valid && pm->pipe_z && pm->ztx > 0) {
+    if ((rc = launch_zpipe_epi<R>(g, tb, *pm, bcor, out, mode, pruned, err, stream, hook, hctx)))
+      return rc;
+  } else {
+    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
     Ptr6 pw{}, pb{}, po{};
     for (int i = 0; i < 3; ++i) {
       pw.p[i] = w[i];
       pb.p[i] = bcor[i];
       po.p[i] = out[i];
     }
-    const dim3 grid = pruned ? dim3(tb.nztiles) : dim3(c.ntiles, g.ny);
+    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZFwdEpi, true);
-    k_zfwd_epi<R><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned);
+    k_zfwd_epi<R><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned, tb.ztl[c.lgTX]);
     GT_HOOK(kKZFwdEpi, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
@@ -878,6 +938,19 @@ int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int
   const int blocks = serial ? 1 : (n + threads - 1) / threads;
   GT_HOOK(kKForce, true);
   k_force<R><<<blocks, threads, 0, (cudaStream_t)stream>>>(pb, entries, n, serial, g);
+  GT_HOOK(kKForce, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_force_indexed(const Geom& g, void* const b[3], const ForceEntry* base, int n,
+                         const int* step, void* stream, LaunchHook hook, void* hctx) {
+  Ptr6 pb{};
+  for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  GT_HOOK(kKForce, true);
+  if (n > 0)
+    k_force_indexed<R><<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(pb, base, n, step, g);
+  k_step_inc<<<1, 32, 0, (cudaStream_t)stream>>>(const_cast<int*>(step));
   GT_HOOK(kKForce, false);
   return (int)cudaGetLastError();
 }
@@ -1014,9 +1087,13 @@ int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], doubl
   return (int)cudaGetLastError();
 }
 
-void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles) {
+int zpass_default_tx(const Geom& g, int csize) {
+  return 1 << strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024).lgTX;
+}
+
+void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles, int tx) {
   const SCfg c = strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024);
-  const int TX = 1 << c.lgTX;
+  const int TX = tx > 0 ? tx : 1 << c.lgTX;
   tiles.clear();
   for (int y = 0; y < g.ny; ++y)
     for (int t = 0; t * TX < xcut[y]; ++t) {
@@ -1057,19 +1134,22 @@ int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3]
 }
 
 const char* kernel_kind_name(int k) {
-  static const char* names[kNumKinds] = {"zinv_curl", "ypass", "xcross", "zfwd_epilogue",
+  static const char* names[kNumKinds] = {"zinv_curl", "yinv", "xcross", "zfwd_epilogue",
                                          "force", "convert", "diag", "diag_final",
-                                         "xc2r_xr2c", "pointwise"};
+                                         "xc2r_xr2c", "pointwise", "yfwd"};
   return (k >= 0 && k < kNumKinds) ? names[k] : "?";
 }
 
 #define GT_INST(R)                                                                              \
   template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
-                             void* const*, void* const*, int, int, void*, LaunchHook, void*);  \
+                             void* const*, void* const*, int, int, const PipeMaps*, int*,      \
+                             void*, LaunchHook, void*);                                         \
   template int launch_count_outside<R>(const Geom&, const DevTables<R>&, void* const*,         \
                                        unsigned long long*, void*);                            \
   template int launch_force<R>(const Geom&, void* const*, const ForceEntry*, int, int, void*,  \
                                LaunchHook, void*);                                              \
+  template int launch_force_indexed<R>(const Geom&, void* const*, const ForceEntry*, int,      \
+                                       const int*, void*, LaunchHook, void*);                  \
   template int launch_convert<R>(const Geom&, const void*, void*, int, void*, LaunchHook,      \
                                  void*);                                                        \
   template int launch_fft_inv<R>(const Geom&, const DevTables<R>&, void*, void*, void* const*, \

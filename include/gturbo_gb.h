@@ -180,6 +180,14 @@ int gt_check_finite(gt_handle* h);
 int gt_set_pruning(gt_handle* h, int32_t enable);
 /* *active = 1 if the next gt_rk2_step takes the pruned path. */
 int gt_pruning_active(gt_handle* h, int32_t* active);
+/* TMA-pipelined y passes (on by default where the device supports them);
+ * off selects the one-tile-per-CTA passes.  Results agree to rounding. */
+int gt_set_pipelining(gt_handle* h, int32_t enable);
+/* Launch-shape tuning (results are unchanged):
+ * "y_tx", "z_tx" (0 = default, or 2/4/8/16: x-columns per block of the y / z passes),
+ * "pipe_y", "pipe_z", "pipe_x" (0/1: TMA-pipelined persistent pass or one tile per block),
+ * "x_pairs" (row pairs per pipelined x-pass block, 1..8), "x_stages" (2..4). */
+int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 
 /* Allocation-free kinetic energy, for callers that cannot allocate device
  * memory: a Fortran driver whose device arrays belong to another runtime (an
@@ -200,6 +208,34 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
 int gt_energy_noalloc(const double* bx, const double* by, const double* bz, int32_t nx,
                       int32_t ny, int32_t nz, double xlx, double xly, double xlz,
                       double* energy_out, void* stream);
+
+/* Launch-shape autotuner: times whole RK2 steps (CUDA events) over the
+ * gt_set_tuning knobs by coordinate descent on a copy of the current state,
+ * keeps the fastest, and appends it to the JSON-lines cache at cache_path
+ * (NULL: no cache), keyed by grid, precision, pruning and GPU name; a cached
+ * choice is applied without timing.  *best_ms (may be NULL) gets the step
+ * time, or -1 when the cache supplied the choice. */
+int gt_autotune(gt_handle* h, const char* cache_path, double* best_ms);
+
+/* ---- ensemble (no reference counterpart: the reference runs one field) ---- */
+typedef struct gt_ensemble gt_ensemble;
+/* n independent members (grids, physics and precision may differ; all on
+ * members[0].device), each with the state and step of a gt_handle. */
+int gt_ensemble_create(int32_t n, const gt_params* members, gt_ensemble** out);
+int gt_ensemble_destroy(gt_ensemble* e);
+int gt_ensemble_set_state(gt_ensemble* e, int32_t member, const double* bx, const double* by,
+                          const double* bz);
+int gt_ensemble_get_state(gt_ensemble* e, int32_t member, double* bx, double* by, double* bz);
+/* nsteps RK2 steps of every member; seeds[n] are the members' forcing seeds
+ * (advanced).  graph = 1: one captured CUDA graph launch per step advances
+ * all members (member kernels run concurrently on their own streams);
+ * graph = 0: the same kernels launched member by member.  The forcing is
+ * drawn on the host in chunks of 64 steps. */
+int gt_ensemble_step(gt_ensemble* e, int32_t nsteps, int32_t* seeds, int32_t graph);
+/* Total kinetic energy of each member (n values). */
+int gt_ensemble_energy(gt_ensemble* e, double* energy);
+/* gt_autotune once per distinct (grid, precision) class, applied to all its members. */
+int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path);
 
 /* ---- introspection ------------------------------------------------------- */
 const char* gt_strerror(int code);

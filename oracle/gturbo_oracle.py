@@ -473,51 +473,164 @@ def nlt(a, bcor, p: Params, wk: Wavenumbers, mask=None, workers=None, return_phy
     return out
 
 
-def step1(a, c, p: Params, wk: Wavenumbers):
-    """c = emk (a + dt2 c); c(1,1,1) = 0 (rkstep.f90:30-48, split = 0)."""
+def step1(a, c, p: Params, wk: Wavenumbers, zero_origin: bool = True):
+    """c = emk (a + dt2 c); c(1,1,1) = 0 (rkstep.f90:30-48, split = 0).
+    ``zero_origin`` = False for a z-slab that does not hold the (0,0,0) mode."""
     dt2 = p.dt2
     out = []
     for ci in range(3):
         re = wk.emk * (a[ci].real + dt2 * c[ci].real)
         im = wk.emk * (a[ci].imag + dt2 * c[ci].imag)
         z = _cplx(re, im)
-        z[0, 0, 0] = 0.0
+        if zero_origin:
+            z[0, 0, 0] = 0.0
         out.append(z)
     return out
 
 
-def step2(a, c, p: Params, wk: Wavenumbers):
+def step2(a, c, p: Params, wk: Wavenumbers, zero_origin: bool = True):
     """a = emk (emk a + dt c); a(1,1,1) = 0 (rkstep.f90:86-104, split = 0)."""
     out = []
     for ci in range(3):
         re = wk.emk * (wk.emk * a[ci].real + p.dt * c[ci].real)
         im = wk.emk * (wk.emk * a[ci].imag + p.dt * c[ci].imag)
         z = _cplx(re, im)
-        z[0, 0, 0] = 0.0
+        if zero_origin:
+            z[0, 0, 0] = 0.0
         out.append(z)
     return out
 
 
-class Oracle:
-    """One simulation in the reference's order of operations (main.f90:121-150)."""
+def _slabs(nz, nthreads):
+    n = max(1, min(nthreads, nz))
+    edges = [nz * i // n for i in range(n + 1)]
+    return [slice(edges[i], edges[i + 1]) for i in range(n)]
 
-    def __init__(self, p: Params, workers=None):
+
+class _SlabWk:
+    """The wavenumber tables restricted to a z-slab (for slab-parallel work)."""
+
+    def __init__(self, wk, sl):
+        self.fkx, self.fky, self.fkz = wk.fkx, wk.fky, wk.fkz[sl]
+        self.k2 = wk.k2[sl]
+
+
+def nlt_threaded(a, bcor, p: Params, wk: Wavenumbers, mask, nthreads: int):
+    """nlt with its pointwise stages run in parallel over z-slabs (NumPy
+    releases the GIL) and the FFTs on nthreads scipy workers.  Every value is
+    computed by the same expression as in ``nlt``, so the result is identical."""
+    from concurrent.futures import ThreadPoolExecutor
+    sls = _slabs(p.nz, nthreads)
+    v = [np.empty_like(a[0]) for _ in range(3)]
+    w = [np.empty_like(a[0]) for _ in range(3)]
+
+    def pre(sl):
+        sw = _SlabWk(wk, sl)
+        cs = curl([a[c][sl] for c in range(3)], sw)
+        for c in range(3):
+            v[c][sl] = cs[c]
+            w[c][sl] = sw.k2 * a[c][sl]
+
+    with ThreadPoolExecutor(len(sls)) as ex:
+        list(ex.map(pre, sls))
+        ur = [fft_inv(v[c], p, nthreads) for c in range(3)]
+        wr = [fft_inv(w[c], p, nthreads) for c in range(3)]
+        cr = [np.empty_like(ur[0]) for _ in range(3)]
+
+        def mid(sl):
+            cc = cross([x[sl] for x in ur], [x[sl] for x in wr])
+            for c in range(3):
+                cr[c][sl] = cc[c]
+
+        list(ex.map(mid, sls))
+        del ur, wr
+        vh = [fft_dir(cr[c], p, nthreads) for c in range(3)]
+        out = [np.empty_like(a[0]) for _ in range(3)]
+
+        def post(sl):
+            sw = _SlabWk(wk, sl)
+            okz = p.omega * sw.fkz[:, None, None]
+            t = []
+            for c in range(3):
+                re = vh[c][sl].real - okz * bcor[c][sl].imag
+                im = vh[c][sl].imag + okz * bcor[c][sl].real
+                t.append(_cplx(re, im))
+            r = invcurl_slab(t, sw, sl.start == 0)
+            for c in range(3):
+                if p.truncate == 1:
+                    r[c][mask[sl]] = 0.0
+                out[c][sl] = r[c]
+
+        list(ex.map(post, sls))
+    return out
+
+
+def invcurl_slab(a, sw, has_origin):
+    """invcurl on a z-slab (the origin mode is left as is, as in produ.f90:83)."""
+    ax, ay, az = a
+    k2 = sw.k2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kx = sw.fkx[None, None, :] / k2
+        ky = sw.fky[None, :, None] / k2
+        kz = sw.fkz[:, None, None] / k2
+    xr = -ky * az.imag + kz * ay.imag
+    xi = ky * az.real - kz * ay.real
+    yr = -kz * ax.imag + kx * az.imag
+    yi = kz * ax.real - kx * az.real
+    zr = -kx * ay.imag + ky * ax.imag
+    zi = kx * ay.real - ky * ax.real
+    out = [_cplx(xr, xi), _cplx(yr, yi), _cplx(zr, zi)]
+    if has_origin:
+        for c in range(3):
+            out[c][0, 0, 0] = a[c][0, 0, 0]
+    return out
+
+
+class Oracle:
+    """One simulation in the reference's order of operations (main.f90:121-150).
+    ``threads`` > 1 runs the pointwise stages slab-parallel (same results)."""
+
+    def __init__(self, p: Params, workers=None, threads: int = 1):
         self.p = p
         self.wk = defk(p)
         self.fm = iniforcing(p, self.wk)
         self.mask = trunc_mask(self.wk) if p.truncate == 1 else None
         self.workers = workers
+        self.threads = threads
 
     def nlt(self, a, bcor):
+        if self.threads > 1:
+            return nlt_threaded(a, bcor, self.p, self.wk, self.mask, self.threads)
         return nlt(a, bcor, self.p, self.wk, self.mask, self.workers)
+
+    def _stage(self, fn, a, c):
+        if self.threads <= 1:
+            return fn(a, c, self.p, self.wk)
+        from concurrent.futures import ThreadPoolExecutor
+        out = [np.empty_like(a[0]) for _ in range(3)]
+        sls = _slabs(self.p.nz, self.threads)
+
+        class _W:
+            pass
+
+        def run(sl):
+            w = _W()
+            w.emk = self.wk.emk[sl]
+            r = fn([x[sl] for x in a], [x[sl] for x in c], self.p, w, zero_origin=(sl.start == 0))
+            for ci in range(3):
+                out[ci][sl] = r[ci]
+
+        with ThreadPoolExecutor(len(sls)) as ex:
+            list(ex.map(run, sls))
+        return out
 
     def rk2_step(self, b, seed):
         """One RK2 step; returns (b_new, seed_new, n1).  ``n1`` is N(b) from the
         first nlt, which ``fluxes`` uses (main.f90:131-137)."""
         n1 = self.nlt(b, b)                       # main.f90:124-131
-        c = step1(b, n1, self.p, self.wk)         # main.f90:141
+        c = self._stage(step1, b, n1)             # main.f90:141
         n2 = self.nlt(c, b)                       # main.f90:144
-        bn = step2(b, n2, self.p, self.wk)        # main.f90:146
+        bn = self._stage(step2, b, n2)            # main.f90:146
         if self.p.forcing in ("3d3c", "2d2c") and self.fm.nf > 0:
             seed = forcing(self.p, self.wk, self.fm, bn, seed)   # main.f90:149
         return bn, seed, n1

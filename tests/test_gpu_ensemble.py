@@ -1,0 +1,83 @@
+"""Ensemble runner (graph-captured and eager) against independent
+simulations, and the launch-shape autotuner with its cache."""
+import numpy as np
+import pytest
+
+from _helpers import configs, initial, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def _members():
+    import gturbo3d_gb300 as g
+    specs = [((16, 16, 16), "fp64", 3.0, 2e-3), ((32, 32, 32), "fp64", 7.0, 1e-3),
+             ((32, 16, 8), "fp64", 1.5, 5e-3), ((32, 32, 32), "mixed", 12.0, 1e-3),
+             ((16, 16, 16), "mixed", 19.0, 3e-3)]
+    params, states = [], []
+    for k, (n, prec, om, nu) in enumerate(specs):
+        gp, _ = configs(n, precision=prec, forcing="3d3c", omega=om, nu=nu, dt=2e-3)
+        gp.famp = g.forcing_amplitude(0.1, gp)
+        params.append(gp)
+        states.append(initial(n, seed=20 + k))
+    return params, states
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_ensemble_matches_individual_runs(lib, graph):
+    import gturbo3d_gb300 as g
+    params, states = _members()
+    seeds = np.arange(100, 100 + len(params), dtype=np.int32)
+    nsteps = 70                                  # crosses the 64-step forcing chunk
+    refs, rseeds = [], []
+    for p, b, s in zip(params, states, seeds):
+        with g.Simulation(p) as sim:
+            sim.set_state(b)
+            rseeds.append(sim.step(nsteps, int(s)))
+            refs.append(sim.get_state())
+    with g.api.Ensemble(params) as ens:
+        for i, b in enumerate(states):
+            ens.set_state(i, b)
+        out_seeds = ens.step(nsteps, seeds, graph=graph)
+        assert list(out_seeds) == rseeds
+        for i in range(len(params)):
+            got = ens.get_state(i)
+            assert relerr(got, refs[i]) < 1e-14, i
+        e = ens.energy()
+    assert np.all(np.isfinite(e)) and np.all(e > 0)
+
+
+def test_ensemble_graph_equals_eager_bitwise(lib):
+    import gturbo3d_gb300 as g
+    params, states = _members()
+    seeds = np.arange(7, 7 + len(params), dtype=np.int32)
+    res = []
+    for graph in (True, False):
+        with g.api.Ensemble(params) as ens:
+            for i, b in enumerate(states):
+                ens.set_state(i, b)
+            ens.step(5, seeds, graph=graph)
+            res.append([ens.get_state(i) for i in range(len(params))])
+    for a, b in zip(*res):
+        for c in range(3):
+            assert np.array_equal(a[c], b[c])
+
+
+def test_autotune_and_cache(lib, tmp_path):
+    import gturbo3d_gb300 as g
+    gp, _ = configs(64, precision="mixed", forcing="3d3c")
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(64, seed=31)
+    cache = str(tmp_path / "tuning.jsonl")
+    with g.Simulation(gp) as tuned, g.Simulation(gp) as plain:
+        tuned.set_state(b0)
+        plain.set_state(b0)
+        ms = g.api.autotune(tuned, cache)
+        assert ms > 0
+        assert relerr(tuned.get_state(), b0) == 0.0          # the state is restored
+        assert g.api.autotune(tuned, cache) == -1.0           # now from the cache
+        s1 = tuned.step(4, 5)
+        s2 = plain.step(4, 5)
+        assert s1 == s2
+        assert relerr(tuned.get_state(), plain.get_state()) < 1e-6
+    text = open(cache).read()
+    assert '"key": "64x64x64/mixed/pruned/' in text
