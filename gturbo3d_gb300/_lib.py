@@ -83,6 +83,10 @@ SIGNATURES = {
     "gt_set_pipelining": (C.c_int, [_vp, C.c_int32]),
     "gt_set_tuning": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "gt_autotune": (C.c_int, [_vp, C.c_char_p, _dp]),
+    "gt_tl_step": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "gt_adj_step": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "gt_objective": (C.c_int, [_vp, C.c_double, _dp]),
+    "gt_gradient": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_double, _dp, _dp, _dp, _dp]),
     "gt_ensemble_create": (C.c_int, [C.c_int32, _P(GtParams), _P(_vp)]),
     "gt_ensemble_destroy": (C.c_int, [_vp]),
     "gt_ensemble_set_state": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),

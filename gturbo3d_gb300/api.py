@@ -297,6 +297,36 @@ class Simulation:
               "gt_set_state_physical")
         return cc.value
 
+    # -- differentiation ----------------------------------------------------
+    def tl_step(self, db):
+        """Tangent-linear RK2 step at the current state."""
+        db = [self._spec_in(x) for x in db]
+        out = [np.empty(self.shape, np.complex128) for _ in range(3)]
+        check(self.lib.gt_tl_step(self.h, *(_dp(x.view(np.float64)) for x in db),
+                                  *(_dp(x.view(np.float64)) for x in out)), "gt_tl_step")
+        return out
+
+    def adj_step(self, lam):
+        """Adjoint RK2 step at the current state."""
+        lam = [self._spec_in(x) for x in lam]
+        out = [np.empty(self.shape, np.complex128) for _ in range(3)]
+        check(self.lib.gt_adj_step(self.h, *(_dp(x.view(np.float64)) for x in lam),
+                                   *(_dp(x.view(np.float64)) for x in out)), "gt_adj_step")
+        return out
+
+    def objective(self, kmin: float) -> float:
+        j = C.c_double()
+        check(self.lib.gt_objective(self.h, kmin, C.byref(j)), "gt_objective")
+        return j.value
+
+    def gradient(self, nsteps: int, seed: int, checkpoint_every: int, kmin: float):
+        """(J, dJ/db0) of the shell energy after nsteps steps (gt_gradient)."""
+        j = C.c_double()
+        out = [np.empty(self.shape, np.complex128) for _ in range(3)]
+        check(self.lib.gt_gradient(self.h, nsteps, seed, checkpoint_every, kmin, C.byref(j),
+                                   *(_dp(x.view(np.float64)) for x in out)), "gt_gradient")
+        return j.value, out
+
     # -- introspection -----------------------------------------------------
     @property
     def stream(self) -> int:

@@ -162,4 +162,86 @@ __device__ __forceinline__ void fft_line(Cplx<R> v[8], int t, int lgL,
   }
 }
 
+// The same transform with the line length fixed at compile time: the stage
+// sequence unrolls (template recursion), so radices, strides, masks and
+// shifts are constants and no per-stage control flow or index arithmetic is
+// left at run time.
+template <int SIGN, typename R, int LGL, int LGNS, typename Idx>
+__device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw,
+                                              Cplx<R>* sm, const Idx& idx) {
+  using C = Cplx<R>;
+  constexpr int REM = LGL - LGNS;
+  constexpr int LR = REM >= 3 ? 3 : REM;
+  constexpr bool LAST = (REM == LR);
+  constexpr int NS = 1 << LGNS;
+  constexpr int T = 1 << (LGL - 3);
+  if constexpr (LR == 3) {
+    const int k = t & (NS - 1);
+    if constexpr (LGNS > 0) {
+      const int step = k << (LGL - LGNS - 3);
+#pragma unroll
+      for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tw[j * step]));
+    }
+    dft8<SIGN, R>(v);
+    if constexpr (!LAST) {
+      const int base = ((t >> LGNS) << (LGNS + 3)) + k;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) sm[idx(base + j * NS)] = v[j];
+    }
+  } else if constexpr (LR == 2) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int b = t + m * T;
+      const int k = b & (NS - 1);
+      if constexpr (LGNS > 0) {
+        const int step = k << (LGL - LGNS - 2);
+        v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tw[step]));
+        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[2 * step]));
+        v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tw[3 * step]));
+      }
+      dft4<SIGN>(v[m], v[m + 2], v[m + 4], v[m + 6]);
+      if constexpr (!LAST) {
+        const int base = ((b >> LGNS) << (LGNS + 2)) + k;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sm[idx(base + j * NS)] = v[m + 2 * j];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int b = t + m * T;
+      const int k = b & (NS - 1);
+      if constexpr (LGNS > 0) {
+        const int step = k << (LGL - LGNS - 1);
+        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[step]));
+      }
+      dft2(v[m], v[m + 4]);
+      if constexpr (!LAST) {
+        const int base = ((b >> LGNS) << (LGNS + 1)) + k;
+        sm[idx(base)] = v[m];
+        sm[idx(base + NS)] = v[m + 4];
+      }
+    }
+  }
+  if constexpr (!LAST) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
+    __syncthreads();
+    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx);
+  }
+}
+
+template <int SIGN, typename R, int LGL, typename Idx>
+__device__ __forceinline__ void fft_line_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw, Cplx<R>* sm,
+                                            const Idx& idx) {
+  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx);
+}
+
+// Strided shared-memory line with a power-of-two tile width.
+struct StridedIdxLg {
+  int lg, x;
+  __device__ __forceinline__ int operator()(int e) const { return (e << lg) + x; }
+};
+
 }  // namespace gt

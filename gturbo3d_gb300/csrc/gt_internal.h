@@ -1,5 +1,5 @@
 // Internal declarations shared by the host set-up code (gt_host.cpp), the
-// kernels (gt_kernels.cu) and the C-ABI (gt_capi.cu).
+// kernels (gt_kernels_impl.cuh, compiled once per precision) and the C-ABI (gt_capi.cu).
 #pragma once
 
 #include <cstddef>
@@ -94,8 +94,8 @@ struct DevTables {
   int nztiles;
   const int32_t* ztiles_p; // the same for the tile width of the pipelined z pass
   int nztiles_p;
-  const int32_t* ztl[5];   // the same for tile widths 1, 2, 4, 8, 16 (tuning)
-  int nztl[5];
+  const int32_t* ztl[11];  // the same for every tile width 2^lg, lg = 0..10
+  int nztl[11];
   int xa;
 };
 
@@ -128,7 +128,7 @@ struct Fields {
   void* w[6];
 };
 
-// Launchers (gt_kernels.cu).  All enqueue on `s` and return cudaError_t as int.
+// Launchers (gt_kernels_impl.cuh).  All enqueue on `s` and return cudaError_t as int.
 struct LaunchRec;  // profiling hook
 using LaunchHook = void (*)(void* ctx, int kind, bool begin);
 
@@ -201,5 +201,12 @@ template <typename R>
 int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], double* partials,
                   int nblocks, double* result, void* stream, LaunchHook hook, void* hctx);
 int diag_blocks(const Geom& g);
+// Tangent-linear / adjoint building blocks (gt_adjoint.cu): out = op(a) [+ beta b].
+template <typename R>
+int launch_spec_op(const Geom& g, const DevTables<R>& tb, void* const out[3], void* const a[3],
+                   void* const b[3], int op, double sgn, double kmin2, double beta, void* stream);
+template <typename R>
+int launch_phys_cross(const Geom& g, void* const out[3], void* const a[3], void* const b[3],
+                      void* const c[3], void* const d[3], double s1, double s2, void* stream);
 
 }  // namespace gt

@@ -32,11 +32,29 @@ namespace gt {
 
 struct Ptr6 {
   void* p[6];
+  // Element i by selects: a run-time index into the parameter array would
+  // make the compiler copy the array to local memory.
+  __device__ __forceinline__ void* at(int i) const {
+    void* r = p[0];
+#pragma unroll
+    for (int k = 1; k < 6; ++k)
+      if (i == k) r = p[k];
+    return r;
+  }
 };
 
 constexpr int kSmemBudget = 200 * 1024;
 
 template <typename R> constexpr int max_threads() { return sizeof(R) == 8 ? 512 : 1024; }
+// x passes: at most 3 x (N/8) x P threads with P row pairs chosen so that the
+// block stays within 256 threads (192 for N <= 512, 384 for N = 1024); the
+// register budget per thread is about 80 (FP32) or 168 (FP64).
+template <int LG> constexpr int xcross_threads() { return LG >= 10 ? 384 : 192; }
+template <typename R, int LG> constexpr int xcross_min_blocks() {
+  return 65536 / (xcross_threads<LG>() * (sizeof(R) == 8 ? 168 : 80)) > 0
+             ? 65536 / (xcross_threads<LG>() * (sizeof(R) == 8 ? 168 : 80))
+             : 1;
+}
 
 static int ilog2i(int n) {
   int l = 0;
@@ -49,7 +67,7 @@ static int ilog2i(int n) {
 // Block: (L/8) x TX threads; thread (t, x) owns positions z = t + i L/8 of
 // column X = tile*TX + x.  Shared memory: three [nz][TX] regions.
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>())
 k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
   using C = Cplx<R>;
@@ -64,14 +82,14 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
   }
   const int X = tile * TX + x;
   const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
-  const int lgL = g.lnz, T = g.nz >> 3;
+  constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = g.nz * TX;
+  const int reg = (1 << LGZ) * TX;
   C* S0 = sm;
   C* S1 = sm + reg;
   C* S2 = sm + 2 * reg;
-  const StridedIdx idx{TX, x};
+  const StridedIdxLg idx{lgTX, x};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   const C* a0 = reinterpret_cast<const C*>(a.p[0]);
   const C* a1 = reinterpret_cast<const C*>(a.p[1]);
@@ -96,7 +114,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
     S2[idx(z)] = uz;
   }
   C* out0 = reinterpret_cast<C*>(w.p[0]);
-  fft_line<+1, R>(v, t, lgL, tw, S0, idx);
+  fft_line_ct<+1, R, LGZ>(v, t, tw, S0, idx);
   if (valid) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) out0[(size_t)(t + i * T) * plane + base] = v[i];
@@ -106,15 +124,15 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
     __syncthreads();
-    fft_line<+1, R>(v, t, lgL, tw, S, idx);
-    C* out = reinterpret_cast<C*>(w.p[f]);
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.at(f));
     if (valid) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
     }
   }
   for (int c = 0; c < 3; ++c) {
-    const C* ac = reinterpret_cast<const C*>(a.p[c]);
+    const C* ac = reinterpret_cast<const C*>(a.at(c));
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int z = t + i * T;
@@ -127,8 +145,8 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
       v[i] = val;
     }
     C* S = c == 0 ? S0 : (c == 1 ? S1 : S2);
-    fft_line<+1, R>(v, t, lgL, tw, S, idx);
-    C* out = reinterpret_cast<C*>(w.p[3 + c]);
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.at(3 + c));
     if (valid) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
@@ -140,9 +158,9 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 // Strided (y or z) transform of up to six fields, in place.  blockIdx.z picks
 // the field, blockIdx.y the outer index (z for a y pass, y for a z pass).
 // ---------------------------------------------------------------------------
-template <typename R, int SIGN>
+template <typename R, int SIGN, int LGL>
 __global__ void __launch_bounds__(max_threads<R>())
-k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, int lgTX, int xlim,
+k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, int xlim,
         int ymask, const int32_t* __restrict__ xcut0) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -151,10 +169,10 @@ k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, in
   const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
   const int X = blockIdx.x * TX + x;
   const bool valid = X < xlim;
-  const int T = 1 << (lgL - 3);
-  C* p = reinterpret_cast<C*>(f.p[blockIdx.z]);
+  constexpr int T = 1 << (LGL - 3);
+  C* p = reinterpret_cast<C*>(f.at(blockIdx.z));
   const size_t base = (size_t)blockIdx.y * (size_t)os + (valid ? X : 0);
-  const StridedIdx idx{TX, x};
+  const StridedIdxLg idx{lgTX, x};
   C v[8];
   // ymask 1 (pruned inverse y pass): only (X, y) with X < xcut0[y] hold data;
   // ymask 2 (pruned forward y pass): only those are stored.
@@ -164,7 +182,7 @@ k_spass(Ptr6 f, Geom g, const void* twv, int lgL, long long ls, long long os, in
     const bool ld = valid && (ymask != 1 || X < xcut0[e]);
     v[i] = ld ? p[base + (size_t)e * (size_t)ls] : C{0, 0};
   }
-  fft_line<SIGN, R>(v, t, lgL, reinterpret_cast<const C*>(twv), sm, idx);
+  fft_line_ct<SIGN, R, LGL>(v, t, reinterpret_cast<const C*>(twv), sm, idx);
   if (valid) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -209,13 +227,13 @@ __device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R
   return first ? C{(a.x + b.x) * s, (a.y - b.y) * s} : C{(a.y + b.y) * s, (b.x - a.x) * s};
 }
 
-template <typename R>
-__global__ void __launch_bounds__(max_threads<R>())
+template <typename R, int LGN>
+__global__ void __launch_bounds__(xcross_threads<LGN>(), (xcross_min_blocks<R, LGN>()))
 k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
-  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  constexpr int N = 1 << LGN, lgN = LGN, lgT = LGN - 3, T = 1 << lgT;
   const int LP = N + (N >> sh);
   const int gid = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const int p = gid / 3, q = gid - 3 * p;
@@ -224,14 +242,15 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   const size_t nhp = g.nhp;
   C v[8];
   // inverse: rows 0 and 1 of the pair, field pair q
+#pragma unroll 1
   for (int r = 0; r < 2; ++r) {
     const size_t row = 2 * pair + r;
-    const C* X1 = reinterpret_cast<const C*>(w.p[2 * q]) + row * nhp;
-    const C* X2 = reinterpret_cast<const C*>(w.p[2 * q + 1]) + row * nhp;
+    const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + row * nhp;
+    const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + row * nhp;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
     const PaddedIdx idx{(p * 6 + r * 3 + q) * LP, sh};
-    fft_line<+1, R>(v, t, lgN, tw, sm, idx);
+    fft_line_ct<+1, R, LGN>(v, t, tw, sm, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
   }
@@ -260,7 +279,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
     __syncthreads();
-    fft_line<-1, R>(v, t, lgN, tw, sm, idx);
+    fft_line_ct<-1, R, LGN>(v, t, tw, sm, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
   }
@@ -269,7 +288,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   // is truncated later (pruned) or xa = nh.
   {
     const int lineA = p * 6 + (q == 2 ? 1 : 0), lineB = p * 6 + (q == 2 ? 1 : 3);
-    C* out = reinterpret_cast<C*>(w.p[q]);
+    C* out = reinterpret_cast<C*>(w.at(q));
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
       const int o = (r == 0 ? lineA : lineB) * LP;
@@ -287,7 +306,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
 // ---------------------------------------------------------------------------
 // Pass 5: forward z transform of three fields, then the spectral epilogue.
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>())
 k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
            const int32_t* __restrict__ tiles) {
@@ -303,19 +322,19 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   }
   const int X = tile * TX + x;
   const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
-  const int lgL = g.lnz, T = g.nz >> 3;
+  constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = g.nz * TX;
-  const StridedIdx idx{TX, x};
+  const int reg = (1 << LGZ) * TX;
+  const StridedIdxLg idx{lgTX, x};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   C v[8];
   for (int f = 0; f < 3; ++f) {
-    const C* in = reinterpret_cast<const C*>(w.p[f]);
+    const C* in = reinterpret_cast<const C*>(w.at(f));
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = valid ? in[(size_t)(t + i * T) * plane + base] : C{0, 0};
     C* S = sm + f * reg;
-    fft_line<-1, R>(v, t, lgL, tw, S, idx);
+    fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
   }
@@ -381,13 +400,13 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 // ---------------------------------------------------------------------------
 // Plain x transforms (rows of one field packed in pairs).
 // ---------------------------------------------------------------------------
-template <typename R>
+template <typename R, int LGN>
 __global__ void __launch_bounds__(max_threads<R>())
 k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, int sh) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
-  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  constexpr int N = 1 << LGN, lgT = LGN - 3, T = 1 << lgT;
   const int LP = N + (N >> sh);
   const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const size_t pair = (size_t)blockIdx.x * P + p;
@@ -397,7 +416,7 @@ k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, 
   C v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, g.nh);
-  fft_line<+1, R>(v, t, lgN, reinterpret_cast<const C*>(twv), sm, PaddedIdx{p * LP, sh});
+  fft_line_ct<+1, R, LGN>(v, t, reinterpret_cast<const C*>(twv), sm, PaddedIdx{p * LP, sh});
   R* r0 = real + (2 * pair) * (size_t)N;
   R* r1 = real + (2 * pair + 1) * (size_t)N;
 #pragma unroll
@@ -407,13 +426,13 @@ k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, 
   }
 }
 
-template <typename R>
+template <typename R, int LGN>
 __global__ void __launch_bounds__(max_threads<R>())
 k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, int sh, R shalf) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
-  const int N = g.nx, lgN = g.lnx, lgT = lgN - 3, T = 1 << lgT;
+  constexpr int N = 1 << LGN, lgT = LGN - 3, T = 1 << lgT;
   const int LP = N + (N >> sh);
   const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const size_t pair = (size_t)blockIdx.x * P + p;
@@ -423,7 +442,7 @@ k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, 
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = C{r0[t + i * T], r1[t + i * T]};
   const PaddedIdx idx{p * LP, sh};
-  fft_line<-1, R>(v, t, lgN, reinterpret_cast<const C*>(twv), sm, idx);
+  fft_line_ct<-1, R, LGN>(v, t, reinterpret_cast<const C*>(twv), sm, idx);
 #pragma unroll
   for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
   __syncthreads();
@@ -511,7 +530,7 @@ __global__ void k_force(Ptr6 b, const ForceEntry* __restrict__ e, int n, int ser
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (!(en.mask & (1 << c))) continue;
-      C* p = reinterpret_cast<C*>(b.p[c]);
+      C* p = reinterpret_cast<C*>(b.at(c));
       if (sizeof(R) == 8) {
         const C v = p[o];
         p[o] = C{(R)((double)v.x + en.inc[2 * c]), (R)((double)v.y + en.inc[2 * c + 1])};
@@ -537,7 +556,7 @@ __global__ void k_force_indexed(Ptr6 b, const ForceEntry* __restrict__ base, int
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (!(en.mask & (1 << c))) continue;
-    C* p = reinterpret_cast<C*>(b.p[c]);
+    C* p = reinterpret_cast<C*>(b.at(c));
     const C v = p[o];
     if (sizeof(R) == 8)
       p[o] = C{(R)((double)v.x + en.inc[2 * c]), (R)((double)v.y + en.inc[2 * c + 1])};
@@ -546,7 +565,7 @@ __global__ void k_force_indexed(Ptr6 b, const ForceEntry* __restrict__ base, int
   }
 }
 
-__global__ void k_step_inc(int* step) {
+static __global__ void k_step_inc(int* step) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
 }
 
@@ -726,7 +745,7 @@ k_energy(Ptr6 bb, DevTables<R> tb, Geom g, double* partials) {
   }
 }
 
-__global__ void k_final_sum(const double* __restrict__ partials, int nblocks, int nq,
+static __global__ void k_final_sum(const double* __restrict__ partials, int nblocks, int nq,
                             double* __restrict__ result) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     double v = 0.0;
@@ -754,7 +773,7 @@ static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads, int for
     c.ntiles = (nh + TX - 1) / TX;
     return c;
   }
-  int TX = 128 / csize;
+  int TX = 64 / csize;   // 64-byte tile rows: two or more blocks per SM (measured best at 512^3)
   while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
   int cap = 1;
   while (cap < nh) cap <<= 1;
@@ -807,16 +826,38 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  const cudaError_t es[] = {
-      allow_smem(k_zinv_curl<R>, optin), allow_smem(k_spass<R, 1>, optin),
-      allow_smem(k_spass<R, -1>, optin), allow_smem(k_xcross<R>, optin),
-      allow_smem(k_zfwd_epi<R>, optin),  allow_smem(k_xc2r<R>, optin),
-      allow_smem(k_xr2c<R>, optin),      allow_smem(k_diag<R>, optin)};
-  for (cudaError_t x : es)
-    if (x != cudaSuccess) return (int)x;
+  cudaError_t es[8 * 7 + 1];
+  int n = 0;
+#define GT_ALLOW(LG)                                     \
+  es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
+  es[n++] = allow_smem(k_spass<R, 1, LG>, optin);        \
+  es[n++] = allow_smem(k_spass<R, -1, LG>, optin);       \
+  es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
+  es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
+  es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
+  es[n++] = allow_smem(k_xr2c<R, LG>, optin);
+  GT_ALLOW(3) GT_ALLOW(4) GT_ALLOW(5) GT_ALLOW(6) GT_ALLOW(7) GT_ALLOW(8) GT_ALLOW(9) GT_ALLOW(10)
+#undef GT_ALLOW
+  es[n++] = allow_smem(k_diag<R>, optin);
+  for (int i = 0; i < n; ++i)
+    if (es[i] != cudaSuccess) return (int)es[i];
   if (dev < 32) done_mask[idx] |= 1u << dev;
   return 0;
 }
+
+// Launches F(LG) for the run-time log2 length lg (3..10).
+#define GT_DISPATCH_LG(lg, F)                                                  \
+  switch (lg) {                                                                \
+    case 3: F(3); break;                                                       \
+    case 4: F(4); break;                                                       \
+    case 5: F(5); break;                                                       \
+    case 6: F(6); break;                                                       \
+    case 7: F(7); break;                                                       \
+    case 8: F(8); break;                                                       \
+    case 9: F(9); break;                                                       \
+    case 10: F(10); break;                                                     \
+    default: return (int)cudaErrorInvalidValue;                                \
+  }
 
 #define GT_HOOK(kind, begin) \
   if (hook) hook(hctx, (kind), (begin))
@@ -840,10 +881,13 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
   dim3 grid((xlim + TX - 1) / TX, outer, nf);
   const int kind = sign > 0 ? kKYPass : kKYFwd;
   GT_HOOK(kind, true);
-  if (sign > 0)
-    k_spass<R, 1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
-  else
-    k_spass<R, -1><<<grid, c.threads, c.smem, s>>>(f, g, tw, lgL, ls, os, c.lgTX, xlim, ymask, xcut0);
+#define GT_L(LG)                                                                                  \
+  if (sign > 0)                                                                                   \
+    k_spass<R, 1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0); \
+  else                                                                                            \
+    k_spass<R, -1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0);
+  GT_DISPATCH_LG(lgL, GT_L)
+#undef GT_L
   GT_HOOK(kind, false);
   return (int)cudaGetLastError();
 }
@@ -860,12 +904,15 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
   // pass 1
   {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
+    if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;   // no tile list
     Ptr6 pa{}, pw{};
     for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
-    k_zinv_curl<R><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
+#define GT_L(LG) k_zinv_curl<R, LG><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
+    GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
     GT_HOOK(kKZinvCurl, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
@@ -887,6 +934,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     const int sh = pad_shift<R>();
     const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6, sh);
     const int threads = 3 * P * (g.nx / 8);
+    if (threads > (g.lnx >= 10 ? 384 : 192)) return (int)cudaErrorInvalidConfiguration;
     const int LP = g.nx + (g.nx >> sh);
     const int smem = 6 * P * LP * csize;
     const long long nblocks = (long long)g.ny * g.nz / 2 / P;
@@ -894,7 +942,9 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
     GT_HOOK(kKXCross, true);
-    k_xcross<R><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf, xlim);
+#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf, xlim);
+    GT_DISPATCH_LG(g.lnx, GT_L)
+#undef GT_L
     GT_HOOK(kKXCross, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
@@ -913,6 +963,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
       return rc;
   } else {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
+    if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;
     Ptr6 pw{}, pb{}, po{};
     for (int i = 0; i < 3; ++i) {
       pw.p[i] = w[i];
@@ -921,7 +972,9 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     }
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZFwdEpi, true);
-    k_zfwd_epi<R><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned, tb.ztl[c.lgTX]);
+#define GT_L(LG) k_zfwd_epi<R, LG><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned, tb.ztl[c.lgTX]);
+    GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
     GT_HOOK(kKZFwdEpi, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
@@ -989,8 +1042,11 @@ int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real
   const int LP = g.nx + (g.nx >> sh);
   const long long nblocks = (long long)g.ny * g.nz / 2 / P;
   GT_HOOK(kKFft1, true);
-  k_xc2r<R><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(
+#define GT_L(LG)                                                                    \
+  k_xc2r<R, LG><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(            \
       spec, reinterpret_cast<R*>(real_out), g, tb.twx, P, sh);
+  GT_DISPATCH_LG(g.lnx, GT_L)
+#undef GT_L
   GT_HOOK(kKFft1, false);
   return (int)cudaGetLastError();
 }
@@ -1009,8 +1065,11 @@ int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, v
   const long long nblocks = (long long)g.ny * g.nz / 2 / P;
   const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
   GT_HOOK(kKFft1, true);
-  k_xr2c<R><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(
+#define GT_L(LG)                                                                    \
+  k_xr2c<R, LG><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(            \
       reinterpret_cast<const R*>(real_in), spec_out, g, tb.twx, P, sh, shalf);
+  GT_DISPATCH_LG(g.lnx, GT_L)
+#undef GT_L
   GT_HOOK(kKFft1, false);
   if ((rc = (int)cudaGetLastError())) return rc;
   void* f[1] = {spec_out};
@@ -1039,11 +1098,13 @@ int launch_point(const Geom& g, const DevTables<R>& tb, void* const a[3], int op
   return (int)cudaGetLastError();
 }
 
+#ifdef GT_KERNELS_COMMON
 int diag_blocks(const Geom& g) {
   const long long rows = (long long)g.ny * g.nz;
   long long b = (rows + 7) / 8;
   return (int)std::min<long long>(b, 152 * 2);
 }
+#endif
 
 template <typename R>
 int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const n1[3],
@@ -1087,6 +1148,7 @@ int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], doubl
   return (int)cudaGetLastError();
 }
 
+#ifdef GT_KERNELS_COMMON
 int zpass_default_tx(const Geom& g, int csize) {
   return 1 << strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024).lgTX;
 }
@@ -1101,6 +1163,7 @@ void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int
       tiles.push_back(y);
     }
 }
+#endif
 
 template <typename R>
 __global__ void k_count_outside(Ptr6 b, DevTables<R> tb, Geom g, unsigned long long* count) {
@@ -1112,7 +1175,7 @@ __global__ void k_count_outside(Ptr6 b, DevTables<R> tb, Geom g, unsigned long l
     for (int X = cut + threadIdx.x; X < g.nh; X += blockDim.x) {
       const size_t o = row * g.nhp + X;
       for (int c = 0; c < 3; ++c) {
-        const C v = reinterpret_cast<const C*>(b.p[c])[o];
+        const C v = reinterpret_cast<const C*>(b.at(c))[o];
         if (v.x != (R)0 || v.y != (R)0) ++n;
       }
     }
@@ -1133,12 +1196,14 @@ int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3]
   return (int)cudaGetLastError();
 }
 
+#ifdef GT_KERNELS_COMMON
 const char* kernel_kind_name(int k) {
   static const char* names[kNumKinds] = {"zinv_curl", "yinv", "xcross", "zfwd_epilogue",
                                          "force", "convert", "diag", "diag_final",
                                          "xc2r_xr2c", "pointwise", "yfwd"};
   return (k >= 0 && k < kNumKinds) ? names[k] : "?";
 }
+#endif
 
 #define GT_INST(R)                                                                              \
   template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
@@ -1164,7 +1229,6 @@ const char* kernel_kind_name(int k) {
                               double, double, double, double, double*, int, double*, void*,    \
                               LaunchHook, void*);
 
-GT_INST(float)
-GT_INST(double)
+GT_INST(GT_REAL)
 
 }  // namespace gt

@@ -209,6 +209,28 @@ int gt_energy_noalloc(const double* bx, const double* by, const double* bz, int3
                       int32_t ny, int32_t nz, double xlx, double xly, double xlz,
                       double* energy_out, void* stream);
 
+/* ---- differentiation (no reference counterpart) ----------------------------
+ * Tangent-linear and adjoint of one RK2 step at the current state (which is
+ * left unchanged), for spectral perturbations / adjoint fields in the host
+ * layout.  Adjoints are taken under <x, y> = sum over stored modes of
+ * w Re(conj(x) y), w = 1 on the kx = 0 and kx = NX/2 planes and 2 elsewhere
+ * (the full-spectrum inner product of real fields).  The forcing is additive
+ * and state-independent, so it has no tangent. */
+int gt_tl_step(gt_handle* h, const double* dbx, const double* dby, const double* dbz,
+               double* ox, double* oy, double* oz);
+int gt_adj_step(gt_handle* h, const double* lx, const double* ly, const double* lz,
+                double* ox, double* oy, double* oz);
+/* J = sum over stored modes with |k| >= kmin of fac |(curl b)_k|^2 (the
+ * kinetic energy of those shells, fac as in glob). */
+int gt_objective(gt_handle* h, double kmin, double* J);
+/* Gradient of J after nsteps RK2 steps from the current state, with the
+ * forcing realisation drawn from `seed` (not advanced), by a checkpointed
+ * adjoint sweep (states stored every checkpoint_every steps and recomputed
+ * per segment).  Writes J and dJ/db0 (so that dJ = <g, db0>); the state is
+ * restored to its initial value. */
+int gt_gradient(gt_handle* h, int32_t nsteps, int32_t seed, int32_t checkpoint_every, double kmin,
+                double* J, double* gx, double* gy, double* gz);
+
 /* Launch-shape autotuner: times whole RK2 steps (CUDA events) over the
  * gt_set_tuning knobs by coordinate descent on a copy of the current state,
  * keeps the fastest, and appends it to the JSON-lines cache at cache_path
