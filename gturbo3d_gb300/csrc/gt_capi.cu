@@ -176,13 +176,35 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   const size_t o_fkxs = putR(ht.fkxs), o_fkys = putR(ht.fkys), o_fkzs = putR(ht.fkzs);
   const size_t o_emk = putR(ht.emk_by_k2 ? ht.emk_k2 : ht.emk_full);
   const size_t o_xcut = put(ht.xcut.data(), ht.xcut.size() * sizeof(int32_t));
+  // Each axis: the full table tw[m] = exp(-2 pi i m / L), m < L, followed by
+  // the per-stage table of the Stockham line transform (tw_stage_offset in
+  // gt_fft.cuh): for every stage after the first (radix r, Ns earlier
+  // points) the entries tw[j k L / (Ns r)] in [j - 1][k] order, so that the
+  // lanes of a warp read consecutive entries.
   auto puttw = [&](int L) {
     std::vector<double> re, im;
     twiddles(L, re, im);
-    std::vector<R> c(2 * L);
+    std::vector<R> c(4 * (size_t)L, (R)0);
     for (int m = 0; m < L; ++m) {
       c[2 * m] = (R)re[m];
       c[2 * m + 1] = (R)im[m];
+    }
+    const int lgl = ilog2(L);
+    size_t off = 0;
+    for (int lgns = 0; lgns < lgl;) {
+      const int lr = lgl - lgns >= 3 ? 3 : lgl - lgns;
+      const int r = 1 << lr, ns = 1 << lgns;
+      if (lgns > 0) {
+        for (int j = 1; j < r; ++j)
+          for (int k = 0; k < ns; ++k) {
+            const size_t m = (size_t)j * k * (L / (ns * r));
+            const size_t e = L + off + (size_t)(j - 1) * ns + k;
+            c[2 * e] = (R)re[m];
+            c[2 * e + 1] = (R)im[m];
+          }
+        off += (size_t)(r - 1) * ns;
+      }
+      lgns += lr;
     }
     return put(c.data(), c.size() * sizeof(R));
   };
@@ -742,6 +764,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "x_stages" && value >= 2 && value <= 4) h->pm.x_stages = value;
   else if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
+  else if (k == "x_fused") h->pm.x_fused = value != 0;
   else return GT_EINVAL;
   return GT_OK;
 }
@@ -832,12 +855,12 @@ const char* gt_last_error(void) { return g_last_error.c_str(); }
 namespace {
 
 struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx;
+  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused;
 };
 
 Tuning get_tuning(const gt_handle* h) {
   return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
-                h->pm.z_tx};
+                h->pm.z_tx, h->pm.x_fused};
 }
 
 void put_tuning(gt_handle* h, const Tuning& t) {
@@ -848,6 +871,7 @@ void put_tuning(gt_handle* h, const Tuning& t) {
   h->pm.x_stages = t.x_stages;
   h->pm.y_tx = t.y_tx;
   h->pm.z_tx = t.z_tx;
+  h->pm.x_fused = t.x_fused;
 }
 
 std::string tuning_key(const gt_handle* h) {
@@ -878,7 +902,7 @@ bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
     };
     if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
         get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
-        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx)) {
+        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused)) {
       t = u;
       found = true;   // the last matching line wins
     }
@@ -893,8 +917,9 @@ void cache_store(const char* path, const std::string& key, const Tuning& t, doub
   if (!f) return;
   std::fprintf(f,
                "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
-               "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"ms_per_step\": %.6f}\n",
-               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, ms);
+               "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
+               "\"ms_per_step\": %.6f}\n",
+               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused, ms);
   std::fclose(f);
 }
 
@@ -951,7 +976,7 @@ int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
   const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
                                    {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
                                    {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
-                                   {&Tuning::x_stages, {2, 3}}};
+                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {
       if (best.*(k.field) == v) continue;
@@ -994,7 +1019,6 @@ enum SpecOp { kOpCurl = 0, kOpK2 = 1, kOpInvcurl = 2, kOpTrunc = 3, kOpCoriolis 
 
 struct F3 {
   void* p[3];
-  void* const* ptr() const { return p; }
 };
 
 template <typename R>

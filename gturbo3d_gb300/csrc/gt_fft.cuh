@@ -162,25 +162,40 @@ __device__ __forceinline__ void fft_line(Cplx<R> v[8], int t, int lgL,
   }
 }
 
+// Offset, within the per-stage twiddle table, of the stage that starts after
+// 2^lgns points: every earlier stage but the first (radix r, Ns points
+// before it) holds (r - 1) Ns entries tw[j k L / (Ns r)] in [j - 1][k] order.
+constexpr int tw_stage_offset(int lgl, int lgns) {
+  int off = 0;
+  for (int s = 0; s < lgns;) {
+    const int lr = lgl - s >= 3 ? 3 : lgl - s;
+    if (s > 0) off += ((1 << lr) - 1) << s;
+    s += lr;
+  }
+  return off;
+}
+
 // The same transform with the line length fixed at compile time: the stage
 // sequence unrolls (template recursion), so radices, strides, masks and
 // shifts are constants and no per-stage control flow or index arithmetic is
-// left at run time.
-template <int SIGN, typename R, int LGL, int LGNS, typename Idx>
+// left at run time.  Twiddles come from the per-stage table stored after the
+// L entries of the full table (`tw + L`), where the lanes of a warp read
+// consecutive entries.
+template <int SIGN, typename R, int LGL, int LGNS, typename Idx, typename Sync>
 __device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw,
-                                              Cplx<R>* sm, const Idx& idx) {
+                                              Cplx<R>* sm, const Idx& idx, const Sync& sync) {
   using C = Cplx<R>;
   constexpr int REM = LGL - LGNS;
   constexpr int LR = REM >= 3 ? 3 : REM;
   constexpr bool LAST = (REM == LR);
   constexpr int NS = 1 << LGNS;
   constexpr int T = 1 << (LGL - 3);
+  const C* tws = tw + (1 << LGL) + tw_stage_offset(LGL, LGNS);
   if constexpr (LR == 3) {
     const int k = t & (NS - 1);
     if constexpr (LGNS > 0) {
-      const int step = k << (LGL - LGNS - 3);
 #pragma unroll
-      for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tw[j * step]));
+      for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tws[(j - 1) * NS + k]));
     }
     dft8<SIGN, R>(v);
     if constexpr (!LAST) {
@@ -194,10 +209,9 @@ __device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>
       const int b = t + m * T;
       const int k = b & (NS - 1);
       if constexpr (LGNS > 0) {
-        const int step = k << (LGL - LGNS - 2);
-        v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tw[step]));
-        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[2 * step]));
-        v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tw[3 * step]));
+        v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tws[k]));
+        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tws[NS + k]));
+        v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tws[2 * NS + k]));
       }
       dft4<SIGN>(v[m], v[m + 2], v[m + 4], v[m + 6]);
       if constexpr (!LAST) {
@@ -211,10 +225,7 @@ __device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>
     for (int m = 0; m < 4; ++m) {
       const int b = t + m * T;
       const int k = b & (NS - 1);
-      if constexpr (LGNS > 0) {
-        const int step = k << (LGL - LGNS - 1);
-        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[step]));
-      }
+      if constexpr (LGNS > 0) v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tws[k]));
       dft2(v[m], v[m + 4]);
       if constexpr (!LAST) {
         const int base = ((b >> LGNS) << (LGNS + 1)) + k;
@@ -224,24 +235,50 @@ __device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>
     }
   }
   if constexpr (!LAST) {
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
-    __syncthreads();
-    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx);
+    sync();
+    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx, sync);
   }
 }
 
-template <int SIGN, typename R, int LGL, typename Idx>
+// Synchronisation of the threads that share one line's scratch.
+struct BlockSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+// A named barrier over `count` threads (a multiple of 32: whole warps).
+struct NamedSync {
+  int id, count;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+};
+
+template <int SIGN, typename R, int LGL, typename Idx, typename Sync = BlockSync>
 __device__ __forceinline__ void fft_line_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw, Cplx<R>* sm,
-                                            const Idx& idx) {
-  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx);
+                                            const Idx& idx, const Sync& sync = Sync{}) {
+  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx, sync);
 }
 
-// Strided shared-memory line with a power-of-two tile width.
+// Strided shared-memory tile of a y or z pass: element e of column x of a
+// [rows][2^lg] tile, with one padding row after every 8 rows.  The padding
+// puts the rows that the threads of one 128-byte phase touch together in a
+// Stockham stage (8 t + j, 8 (t + 1) + j, ...) into different banks.
+__host__ __device__ constexpr int strided_rows(int L) { return L + (L >> 3); }
 struct StridedIdxLg {
   int lg, x;
-  __device__ __forceinline__ int operator()(int e) const { return (e << lg) + x; }
+  __device__ __forceinline__ int operator()(int e) const { return ((e + (e >> 3)) << lg) + x; }
+};
+
+// Contiguous line of an x pass, XOR-swizzled within aligned groups of 16
+// elements: bits 0..3 of e take bits 3..6 of e.  A bijection on each group,
+// so the line needs no padding; it spreads the Stockham stage writes of a
+// 128-byte phase over all banks for 8- and 16-byte elements.
+__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 3) & 15); }
+struct SwzIdx {
+  int off;
+  __device__ __forceinline__ int operator()(int e) const { return off + swz(e); }
 };
 
 }  // namespace gt

@@ -85,7 +85,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = (1 << LGZ) * TX;
+  const int reg = strided_rows(1 << LGZ) * TX;
   C* S0 = sm;
   C* S1 = sm + reg;
   C* S2 = sm + 2 * reg;
@@ -158,8 +158,14 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 // Strided (y or z) transform of up to six fields, in place.  blockIdx.z picks
 // the field, blockIdx.y the outer index (z for a y pass, y for a z pass).
 // ---------------------------------------------------------------------------
+// At most 256 threads per block; for FP32 five resident blocks (48
+// registers), which hides more load latency than four blocks of 64 registers
+// (measured at 512^3: inverse y pass 1.04 ms against 1.11 ms).
+constexpr int kSpassThreads = 256;
+template <typename R> constexpr int spass_min_blocks() { return sizeof(R) == 8 ? 2 : 5; }
+
 template <typename R, int SIGN, int LGL>
-__global__ void __launch_bounds__(max_threads<R>())
+__global__ void __launch_bounds__(kSpassThreads, spass_min_blocks<R>())
 k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, int xlim,
         int ymask, const int32_t* __restrict__ xcut0) {
   using C = Cplx<R>;
@@ -229,12 +235,12 @@ __device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R
 
 template <typename R, int LGN>
 __global__ void __launch_bounds__(xcross_threads<LGN>(), (xcross_min_blocks<R, LGN>()))
-k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
+k_xcross(Ptr6 w, Geom g, const void* twv, int P, R shalf, int xa) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int N = 1 << LGN, lgN = LGN, lgT = LGN - 3, T = 1 << lgT;
-  const int LP = N + (N >> sh);
+  constexpr int LP = N;
   const int gid = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const int p = gid / 3, q = gid - 3 * p;
   const size_t pair = (size_t)blockIdx.x * P + p;
@@ -249,7 +255,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
     const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + row * nhp;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
-    const PaddedIdx idx{(p * 6 + r * 3 + q) * LP, sh};
+    const SwzIdx idx{(p * 6 + r * 3 + q) * LP};
     fft_line_ct<+1, R, LGN>(v, t, tw, sm, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
@@ -259,7 +265,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   // w = (z1.y, z2.x, z2.y) for row 0 and (z3..z5) for row 1.
   for (int n = threadIdx.x; n < P * N; n += blockDim.x) {
     const int pp = n >> lgN, e = n & (N - 1);
-    const int o = pp * 6 * LP + e + (e >> sh);
+    const int o = pp * 6 * LP + swz(e);
     const C z0 = sm[o], z1 = sm[o + LP], z2 = sm[o + 2 * LP];
     const C z3 = sm[o + 3 * LP], z4 = sm[o + 4 * LP], z5 = sm[o + 5 * LP];
     const R c0x = z0.y * z2.y - z1.x * z2.x;
@@ -275,7 +281,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
   __syncthreads();
   {
     const int line = p * 6 + (q == 0 ? 0 : (q == 1 ? 3 : 1));
-    const PaddedIdx idx{line * LP, sh};
+    const SwzIdx idx{line * LP};
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
     __syncthreads();
@@ -296,10 +302,103 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, int sh, R shalf, int xa) {
       C* orow = out + (2 * pair + r) * nhp;
       for (int k = t; k < xa; k += T) {
         const int kb = (N - k) & (N - 1);
-        const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
+        const C a = sm[o + swz(k)], b = sm[o + swz(kb)];
         orow[k] = split_r2c<R>(a, b, first, shalf);
       }
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3, register-resident form: one group of N/8 threads owns a whole pair
+// of rows.  It runs the three packed inverse transforms of row 0 one after the
+// other, keeping the first two results in registers, so that u x w is formed
+// in registers in the natural order the last Stockham stage leaves; the
+// packed line c_x + i c_y goes straight into the forward transform, c_z waits
+// in registers for row 1 and is packed with it.  Shared memory is used only
+// for the transforms' own exchanges and for the r2c split (which needs
+// Z[k] and Z[N-k]): 41 N line accesses per row pair instead of 61 N.  Groups
+// synchronise on their own named barrier when they fill whole warps.
+// ---------------------------------------------------------------------------
+template <typename R> constexpr int xfused_threads() { return sizeof(R) == 8 ? 128 : 256; }
+
+template <typename R, int LGN>
+__global__ void __launch_bounds__(xfused_threads<R>(), 2)
+k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
+  using C = Cplx<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int N = 1 << LGN, T = N / 8;
+  constexpr int LP = N;
+  const int grp = threadIdx.x >> (LGN - 3), t = threadIdx.x & (T - 1);
+  const int P = blockDim.x >> (LGN - 3);
+  const size_t pair = (size_t)blockIdx.x * P + grp;
+  const C* tw = reinterpret_cast<const C*>(twv);
+  const size_t nhp = g.nhp;
+  const SwzIdx idx{grp * LP};
+  C* line = sm + grp * LP;
+  C v[8], z0[8], z1[8];
+  R cz0[8];
+  auto run = [&](auto sync) {
+#pragma unroll 1
+    for (int r = 0; r < 2; ++r) {
+      const size_t row = 2 * pair + r;
+#pragma unroll 1
+      for (int q = 0; q < 3; ++q) {
+        const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + row * nhp;
+        const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + row * nhp;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
+        fft_line_ct<+1, R, LGN>(v, t, tw, sm, idx, sync);
+        if (q == 0) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) z0[i] = v[i];
+        } else if (q == 1) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) z1[i] = v[i];
+        }
+      }
+      // u = (z0.x, z0.y, z1.x), w = (z1.y, v.x, v.y) (produ.f90:14-16)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const R cx = z0[i].y * v[i].y - z1[i].x * v[i].x;
+        const R cy = z1[i].x * z1[i].y - z0[i].x * v[i].y;
+        const R cz = z0[i].x * v[i].x - z0[i].y * z1[i].y;
+        if (r == 0) {
+          cz0[i] = cz;
+        } else {
+          z1[i] = C{cz0[i], cz};
+        }
+        v[i] = C{cx, cy};
+      }
+      // forward c_x + i c_y of this row -> fields 0 and 1
+#pragma unroll 1
+      for (int pass = 0; pass < (r == 0 ? 1 : 2); ++pass) {
+        if (pass == 1) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = z1[i];
+        }
+        fft_line_ct<-1, R, LGN>(v, t, tw, sm, idx, sync);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
+        sync();
+        // pass 0: Z = c_x + i c_y of row r; pass 1: Z = c_z(row 0) + i c_z(row 1)
+        C* oa = reinterpret_cast<C*>(pass == 0 ? w.p[0] : w.p[2]) + (pass == 0 ? row : 2 * pair) * nhp;
+        C* ob = reinterpret_cast<C*>(pass == 0 ? w.p[1] : w.p[2]) + (pass == 0 ? row : 2 * pair + 1) * nhp;
+        for (int k = t; k < xa; k += T) {
+          const int kb = (N - k) & (N - 1);
+          const C a = line[swz(k)], b = line[swz(kb)];
+          oa[k] = split_r2c<R>(a, b, true, shalf);
+          ob[k] = split_r2c<R>(a, b, false, shalf);
+        }
+        sync();
+      }
+    }
+  };
+  if constexpr (T >= 32) {
+    run(NamedSync{1 + grp, T});
+  } else {
+    run(BlockSync{});
   }
 }
 
@@ -325,7 +424,7 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
   const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = (1 << LGZ) * TX;
+  const int reg = strided_rows(1 << LGZ) * TX;
   const StridedIdxLg idx{lgTX, x};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   C v[8];
@@ -402,12 +501,12 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 // ---------------------------------------------------------------------------
 template <typename R, int LGN>
 __global__ void __launch_bounds__(max_threads<R>())
-k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, int sh) {
+k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int N = 1 << LGN, lgT = LGN - 3, T = 1 << lgT;
-  const int LP = N + (N >> sh);
+  constexpr int LP = N;
   const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const size_t pair = (size_t)blockIdx.x * P + p;
   const C* spec = reinterpret_cast<const C*>(specv);
@@ -416,7 +515,7 @@ k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, 
   C v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, g.nh);
-  fft_line_ct<+1, R, LGN>(v, t, reinterpret_cast<const C*>(twv), sm, PaddedIdx{p * LP, sh});
+  fft_line_ct<+1, R, LGN>(v, t, reinterpret_cast<const C*>(twv), sm, SwzIdx{p * LP});
   R* r0 = real + (2 * pair) * (size_t)N;
   R* r1 = real + (2 * pair + 1) * (size_t)N;
 #pragma unroll
@@ -428,12 +527,12 @@ k_xc2r(const void* specv, R* __restrict__ real, Geom g, const void* twv, int P, 
 
 template <typename R, int LGN>
 __global__ void __launch_bounds__(max_threads<R>())
-k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, int sh, R shalf) {
+k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, R shalf) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int N = 1 << LGN, lgT = LGN - 3, T = 1 << lgT;
-  const int LP = N + (N >> sh);
+  constexpr int LP = N;
   const int p = threadIdx.x >> lgT, t = threadIdx.x & (T - 1);
   const size_t pair = (size_t)blockIdx.x * P + p;
   const R* r0 = real + (2 * pair) * (size_t)N;
@@ -441,7 +540,7 @@ k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, 
   C v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = C{r0[t + i * T], r1[t + i * T]};
-  const PaddedIdx idx{p * LP, sh};
+  const SwzIdx idx{p * LP};
   fft_line_ct<-1, R, LGN>(v, t, reinterpret_cast<const C*>(twv), sm, idx);
 #pragma unroll
   for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
@@ -452,7 +551,7 @@ k_xr2c(const R* __restrict__ real, void* specv, Geom g, const void* twv, int P, 
     const int k = n % nh, rest = n / nh, r = rest & 1, pp = rest >> 1;
     const int o = pp * LP;
     const int kb = (N - k) & (N - 1);
-    const C a = sm[o + k + (k >> sh)], b = sm[o + kb + (kb >> sh)];
+    const C a = sm[o + swz(k)], b = sm[o + swz(kb)];
     const size_t row = 2 * ((size_t)blockIdx.x * P + pp) + r;
     spec[row * g.nhp + k] = split_r2c<R>(a, b, r == 0, shalf);
   }
@@ -763,36 +862,37 @@ struct SCfg {
 
 static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads, int force_tx = 0) {
   const int T = L / 8;
+  const int LR = strided_rows(L);   // shared-memory rows of one field (padded)
   if (force_tx > 0) {
     int TX = force_tx;
-    while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
+    while (TX > 1 && (T * TX > maxthreads || F * LR * TX * csize > kSmemBudget)) TX >>= 1;
     SCfg c;
     c.lgTX = ilog2i(TX);
     c.threads = T * TX;
-    c.smem = F * L * TX * csize;
+    c.smem = F * LR * TX * csize;
     c.ntiles = (nh + TX - 1) / TX;
     return c;
   }
   int TX = 64 / csize;   // 64-byte tile rows: two or more blocks per SM (measured best at 512^3)
-  while (TX > 1 && (T * TX > maxthreads || F * L * TX * csize > kSmemBudget)) TX >>= 1;
+  while (TX > 1 && (T * TX > maxthreads || F * LR * TX * csize > kSmemBudget)) TX >>= 1;
   int cap = 1;
   while (cap < nh) cap <<= 1;
-  while (T * TX * 2 <= 256 && TX * 2 <= cap && F * L * TX * 2 * csize <= kSmemBudget &&
+  while (T * TX * 2 <= 256 && TX * 2 <= cap && F * LR * TX * 2 * csize <= kSmemBudget &&
          T * TX * 2 <= maxthreads)
     TX <<= 1;
   SCfg c;
   c.lgTX = ilog2i(TX);
   c.threads = T * TX;
-  c.smem = F * L * TX * csize;
+  c.smem = F * LR * TX * csize;
   c.ntiles = (nh + TX - 1) / TX;
   return c;
 }
 
-// Pairs of rows per block for the x passes, and the padding shift.
+// Pairs of rows per block for the x passes.
 static int xpass_pairs(const Geom& g, int groups_per_pair, int csize, int maxthreads,
-                       int lines_per_pair, int sh) {
+                       int lines_per_pair) {
   const int T = g.nx / 8;
-  const int LP = g.nx + (g.nx >> sh);
+  const int LP = g.nx;
   const long long npairs = (long long)g.ny * g.nz / 2;
   int P = 1;
   while (P * 2 <= npairs && groups_per_pair * T * P * 2 <= maxthreads &&
@@ -801,8 +901,6 @@ static int xpass_pairs(const Geom& g, int groups_per_pair, int csize, int maxthr
     P <<= 1;
   return P;
 }
-
-template <typename R> static int pad_shift() { return sizeof(R) == 8 ? 3 : 4; }
 
 // Opt-in dynamic shared memory: the device's per-block maximum minus the
 // kernel's static shared memory, set once per (device, precision).
@@ -873,13 +971,14 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
   const long long ls = axis == 1 ? g.nhp : plane;
   const long long os = axis == 1 ? plane : g.nhp;
   const int outer = axis == 1 ? g.nz : g.ny;
-  SCfg c = strided_cfg(L, g.nh, 1, csize, max_threads<R>(), force_tx);
+  SCfg c = strided_cfg(L, g.nh, 1, csize, kSpassThreads, force_tx);
   if (xlim < 0) xlim = g.nh;
   const int TX = 1 << c.lgTX;
   Ptr6 f{};
   for (int i = 0; i < nf; ++i) f.p[i] = fields[i];
-  dim3 grid((xlim + TX - 1) / TX, outer, nf);
+  const int ntx = (xlim + TX - 1) / TX;
   const int kind = sign > 0 ? kKYPass : kKYFwd;
+  dim3 grid(ntx, outer, nf);
   GT_HOOK(kind, true);
 #define GT_L(LG)                                                                                  \
   if (sign > 0)                                                                                   \
@@ -917,32 +1016,52 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     if ((rc = (int)cudaGetLastError())) return rc;
   }
   const int xlim = pruned ? tb.xa : g.nh;
+  // y passes: 32-byte tile rows for FP32 by default (measured best at 512^3)
+  const int ytx = pm && pm->y_tx ? pm->y_tx : (sizeof(R) == 4 ? 4 : 0);
   // pass 2
   if (pm && pm->valid && pm->pipe_y) {
     if ((rc = launch_ypipe<R>(g, *pm, w, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
                               hook, hctx)))
       return rc;
   } else if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
-                            pm ? pm->y_tx : 0))) {
+                            ytx))) {
     return rc;
   }
   // pass 3
   if (pm && pm->valid && pm->pipe_x) {
     if ((rc = launch_xpipe<R>(g, w, tb.twx, xlim, pm->x_pairs, pm->x_stages, err, stream, hook, hctx)))
       return rc;
+  } else if (!pm || pm->x_fused) {
+    // one group of nx/8 threads per row pair; as many groups per block as fit
+    // in xfused_threads and divide the number of row pairs
+    const int T = g.nx / 8;
+    const long long npairs = (long long)g.ny * g.nz / 2;
+    int P = 1;
+    while (P * 2 * T <= xfused_threads<R>() && npairs % (P * 2) == 0) P <<= 1;
+    if (P * T > xfused_threads<R>() || npairs % P != 0) return (int)cudaErrorInvalidConfiguration;
+    const int LP = g.nx;
+    const int smem = P * LP * csize;
+    Ptr6 pw{};
+    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
+    const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
+    GT_HOOK(kKXCross, true);
+#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, g, tb.twx, shalf, xlim);
+    GT_DISPATCH_LG(g.lnx, GT_L)
+#undef GT_L
+    GT_HOOK(kKXCross, false);
+    if ((rc = (int)cudaGetLastError())) return rc;
   } else {
-    const int sh = pad_shift<R>();
-    const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6, sh);
+    const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6);
     const int threads = 3 * P * (g.nx / 8);
     if (threads > (g.lnx >= 10 ? 384 : 192)) return (int)cudaErrorInvalidConfiguration;
-    const int LP = g.nx + (g.nx >> sh);
+    const int LP = g.nx;
     const int smem = 6 * P * LP * csize;
     const long long nblocks = (long long)g.ny * g.nz / 2 / P;
     Ptr6 pw{};
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
     GT_HOOK(kKXCross, true);
-#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, sh, shalf, xlim);
+#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, shalf, xlim);
     GT_DISPATCH_LG(g.lnx, GT_L)
 #undef GT_L
     GT_HOOK(kKXCross, false);
@@ -954,7 +1073,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
                               hook, hctx)))
       return rc;
   } else if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
-                            pm ? pm->y_tx : 0))) {
+                            ytx))) {
     return rc;
   }
   // pass 5
@@ -1037,14 +1156,13 @@ int launch_fft_inv(const Geom& g, const DevTables<R>& tb, void* spec, void* real
   if ((rc = spass<R>(g, f, 1, tb.twz, 2, +1, s, hook, hctx))) return rc;
   if ((rc = spass<R>(g, f, 1, tb.twy, 1, +1, s, hook, hctx))) return rc;
   const int csize = sizeof(Cplx<R>);
-  const int sh = pad_shift<R>();
-  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1, sh);
-  const int LP = g.nx + (g.nx >> sh);
+  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1);
+  const int LP = g.nx;
   const long long nblocks = (long long)g.ny * g.nz / 2 / P;
   GT_HOOK(kKFft1, true);
 #define GT_L(LG)                                                                    \
   k_xc2r<R, LG><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(            \
-      spec, reinterpret_cast<R*>(real_out), g, tb.twx, P, sh);
+      spec, reinterpret_cast<R*>(real_out), g, tb.twx, P);
   GT_DISPATCH_LG(g.lnx, GT_L)
 #undef GT_L
   GT_HOOK(kKFft1, false);
@@ -1059,15 +1177,14 @@ int launch_fft_dir(const Geom& g, const DevTables<R>& tb, const void* real_in, v
   cudaStream_t s = (cudaStream_t)stream;
   (void)w;
   const int csize = sizeof(Cplx<R>);
-  const int sh = pad_shift<R>();
-  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1, sh);
-  const int LP = g.nx + (g.nx >> sh);
+  const int P = xpass_pairs(g, 1, csize, max_threads<R>(), 1);
+  const int LP = g.nx;
   const long long nblocks = (long long)g.ny * g.nz / 2 / P;
   const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
   GT_HOOK(kKFft1, true);
 #define GT_L(LG)                                                                    \
   k_xr2c<R, LG><<<(unsigned)nblocks, P * (g.nx / 8), P * LP * csize, s>>>(            \
-      reinterpret_cast<const R*>(real_in), spec_out, g, tb.twx, P, sh, shalf);
+      reinterpret_cast<const R*>(real_in), spec_out, g, tb.twx, P, shalf);
   GT_DISPATCH_LG(g.lnx, GT_L)
 #undef GT_L
   GT_HOOK(kKFft1, false);
