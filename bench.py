@@ -43,15 +43,17 @@ N = 512           # --size overrides (small cases for profiling only)
 PHYS = dict(nu=2e-4, omega=5.0, dt=1e-3)
 SEED = 2
 INJECTION = 0.1
-METRIC = "RK2 steps/s @512^3 (mixed FP32/FP64 form; FP64 plain form and rel. energy error reported beside)"
+METRIC_FMT = "RK2 steps/s @{n}^3 (mixed FP32/FP64 form; FP64 plain form and rel. energy error reported beside)"
+METRIC = METRIC_FMT.format(n=N)
 UNIT = "steps/s"
 
 
 def workload_config(extra=None):
+    ws_gb = 12 * N * N * (N // 2 + 1) * 8 / 1e9
     c = {"workload": f"rk2_step_{N}cubed_roofline_config", "grid": [N, N, N], "nu": PHYS["nu"],
          "omega": PHYS["omega"], "dt": PHYS["dt"], "forcing": "3d3c k in (1.999,3] injection 0.1",
          "seed": SEED, "dt2_mode": "rk2", "truncate": 1,
-         "l2_flush": "not needed: 12-field working set (6.6 GB) >> 129 MB L2"}
+         "l2_flush": f"not needed: 12-field working set ({ws_gb:.1f} GB) >> 129 MB L2"}
     if extra:
         c.update(extra)
     return c
@@ -379,7 +381,7 @@ def run_ours(args):
         per_launch_bytes = pbytes[name]
         avg_s = tms / nl / 1e3
         achieved = per_launch_bytes / avg_s / 1e9
-        traffic = ncu_traffic().get((name, "mixed"))
+        traffic = ncu_traffic().get((name, "mixed")) if N == 512 else None
         step_bytes = 2 * sum(pbytes[k] for k in ("zinv_curl", "yinv", "xcross", "yfwd", "zfwd_epilogue"))
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
@@ -413,6 +415,189 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Further synthetic configurations (--workload); each prints one JSON line.
+# ---------------------------------------------------------------------------
+def _event_ms(fn, stream, torch):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_precision(args):
+    """256^3, 2D2C forcing, 200 steps: plain FP64 against mixed; steps/s of
+    both and the mixed form's relative error in energy, helicity, viscous
+    dissipation and the shell spectrum E(k), against the FP64 form (which
+    matches the FP64 oracle step by step, tests/test_gpu_golden.py)."""
+    import numpy as np
+    import torch
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300.synth import initial_potential
+    from gturbo3d_gb300.workloads import precision_params
+    n, nsteps, seed = args.size if args.size != 512 else 256, args.steps if args.steps != 20 else 200, 1
+    b0 = initial_potential(n, n, n, seed)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with g.Simulation(precision_params(prec, n)) as sim:
+            sim.set_state(b0)
+            st = torch.cuda.ExternalStream(sim.stream)
+            ms = _event_ms(lambda: sim.step(nsteps, seed), st, torch)
+            d = sim.diagnostics(flux=False)
+            res[prec] = {"steps_per_s": nsteps / (ms / 1e3), "energy": float(d["energy"][:3].sum()),
+                         "helicity": float(d["helicity"]), "dissipation": float(d["energy"][3:6].sum()),
+                         "spectrum": d["spectrum"]}
+    r64, r32 = res["fp64"], res["mixed"]
+    ek64, ek32 = r64["spectrum"], r32["spectrum"]
+    sig = ek64 > 1e-12 * ek64.max()
+    rel = lambda a, b: abs(a - b) / abs(b) if b != 0 else None
+    line = {"metric": f"RK2 steps/s @{n}^3 2D2C, mixed vs FP64 diagnostics error after {nsteps} steps",
+            "value": r32["steps_per_s"], "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": 0,
+            "higher_is_better": True, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 1)",
+            "config": {"workload": f"rk2_step_{n}cubed_2d2c_precision", "grid": [n] * 3, "nu": 5e-4,
+                       "omega": 10.0, "dt": 2e-3, "forcing": "2d2c kz=0, 2<=|k_h|<=3, injection 0.1",
+                       "seed": seed},
+            "fp64": {"value": r64["steps_per_s"], "unit": UNIT},
+            "mixed_over_fp64": r32["steps_per_s"] / r64["steps_per_s"],
+            "rel_err_mixed_vs_fp64": {"energy": rel(r32["energy"], r64["energy"]),
+                                      "helicity": rel(r32["helicity"], r64["helicity"]),
+                                      "dissipation": rel(r32["dissipation"], r64["dissipation"]),
+                                      "spectrum_max_over_shells": float(np.max(np.abs(ek32[sig] - ek64[sig]) / ek64[sig])),
+                                      "spectrum_shells_compared": int(sig.sum())},
+            "values_fp64": {k: r64[k] for k in ("energy", "helicity", "dissipation")}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ensemble(args):
+    """48 x 64^3 + 12 x 128^3 + 4 x 256^3 mixed members (seeds 100..163,
+    Omega in [1, 20], nu from k_max eta = 1.5, dt from CFL 0.5), 500 steps:
+    one captured CUDA graph launch per step after the autotuner chose each
+    grid class's tiles, against one launch sequence per member per step with
+    default tiles.  value = member-steps/s of the graph mode."""
+    import numpy as np
+    import torch
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300.workloads import ensemble_members, ensemble_params
+    nsteps = args.steps if args.steps != 20 else 500
+    members = ensemble_members()
+    params = ensemble_params(members)
+    seeds0 = np.array([m["seed"] for m in members], np.int32)
+    out = {}
+    for mode in ("graph_autotuned", "per_member_default"):
+        with g.Ensemble(params) as ens:
+            for i, m in enumerate(members):
+                ens.set_state(i, m["b0"])
+            if mode == "graph_autotuned":
+                t0 = time.perf_counter()
+                ens.autotune(None)
+                tune_s = time.perf_counter() - t0
+                for i, m in enumerate(members):
+                    ens.set_state(i, m["b0"])
+            graph = mode == "graph_autotuned"
+            ens.step(args.warmup, seeds0.copy(), graph=graph)      # warm-up (graph capture)
+            for i, m in enumerate(members):
+                ens.set_state(i, m["b0"])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ens.step(nsteps, seeds0.copy(), graph=graph)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            e = ens.energy()
+            out[mode] = {"member_steps_per_s": len(members) * nsteps / dt, "seconds": dt,
+                         "energy_min": float(e.min()), "energy_max": float(e.max()),
+                         "finite": bool(np.isfinite(e).all())}
+            if graph:
+                out[mode]["autotune_seconds"] = tune_s
+    v = out["graph_autotuned"]["member_steps_per_s"]
+    line = {"metric": "ensemble member-steps/s (64 members of 64^3/128^3/256^3, mixed), one graph launch per step",
+            "value": v, "unit": "member-steps/s", "n_gpus": 1, "steps": nsteps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) fields, seeds 100..163)",
+            "config": {"workload": "ensemble_48x64_12x128_4x256", "members": len(members),
+                       "grids": {"64": 48, "128": 12, "256": 4}, "omega_range": [1, 20],
+                       "nu": {str(n): next(m["nu"] for m in members if m["n"] == n) for n in (64, 128, 256)},
+                       "dt": {str(n): [min(m["dt"] for m in members if m["n"] == n),
+                                       max(m["dt"] for m in members if m["n"] == n)] for n in (64, 128, 256)},
+                       "forcing": "3d3c 2<|k|<=3 injection 0.1"},
+            "modes": out,
+            "speedup_graph_autotuned_vs_per_member": v / out["per_member_default"]["member_steps_per_s"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_adjoint(args):
+    """128^3, 200 steps, forcing realisation of seed 3, J = kinetic energy of
+    the shells |k| >= 20 after the run, gradient w.r.t. the initial vector
+    potential with checkpoints every 20 steps.  FP64: TL/adjoint dot product
+    of one step and central differences (h = 1e-6) along 8 seeded random
+    directions; mixed: its gradient against the FP64 gradient."""
+    import numpy as np
+    import torch
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300.synth import initial_potential
+    from gturbo3d_gb300.workloads import adjoint_params, random_direction, spectral_inner
+    n = args.size if args.size != 512 else 128
+    nsteps = args.steps if args.steps != 20 else 200
+    seed, every, kmin, h = 3, 20, 20.0, 1e-6
+    b0 = initial_potential(n, n, n, seed)
+    res = {}
+    grads = {}
+    for prec in ("fp64", "mixed"):
+        with g.Simulation(adjoint_params(prec, n)) as sim:
+            sim.set_state(b0)
+            st = torch.cuda.ExternalStream(sim.stream)
+            t0 = time.perf_counter()
+            J, gr = sim.gradient(nsteps, seed, every, kmin)
+            tg = time.perf_counter() - t0
+            fwd_ms = _event_ms(lambda: sim.step(nsteps, seed), st, torch)
+            sim.set_state(b0)
+            grads[prec] = gr
+            r = {"J": J, "gradient_seconds": tg, "forward_seconds": fwd_ms / 1e3,
+                 "gradient_over_forward": tg / (fwd_ms / 1e3)}
+            if prec == "fp64":
+                x = random_direction(n, 500, scale_to=b0)
+                y = random_direction(n, 501, scale_to=b0)
+                lhs = spectral_inner(y, sim.tl_step(x))
+                rhs = spectral_inner(sim.adj_step(y), x)
+                r["dot_product_rel"] = abs(lhs - rhs) / max(abs(lhs), abs(rhs))
+
+                def Jof(b):
+                    sim.set_state(b)
+                    sim.step(nsteps, seed)
+                    return sim.objective(kmin)
+
+                errs = []
+                for k in range(8):
+                    d = random_direction(n, 600 + k, scale_to=b0)
+                    fd = (Jof([b + h * x for b, x in zip(b0, d)]) - Jof([b - h * x for b, x in zip(b0, d)])) / (2 * h)
+                    ad = spectral_inner(gr, d)
+                    errs.append(abs(fd - ad) / max(abs(fd), 1e-300))
+                r["fd_rel_err"] = errs
+                r["fd_rel_err_max"] = max(errs)
+            res[prec] = r
+    g64, g32 = grads["fp64"], grads["mixed"]
+    num = sum(float(np.sum(np.abs(a - b) ** 2)) for a, b in zip(g32, g64))
+    den = sum(float(np.sum(np.abs(b) ** 2)) for b in g64)
+    line = {"metric": f"adjoint gradient @{n}^3, {nsteps} steps: max rel. error vs central differences (FP64)",
+            "value": res["fp64"]["fd_rel_err_max"], "unit": "relative error", "n_gpus": 1, "steps": nsteps,
+            "warmup": 0, "higher_is_better": False, "dtype": "f64 (plain form); f32 mixed form reported beside",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 3; directions seeds 600..607)",
+            "config": {"workload": f"adjoint_{n}cubed", "grid": [n] * 3, "nu": 1e-3, "omega": 5.0, "dt": 4e-3,
+                       "forcing": "3d3c realisation of seed 3", "objective": "kinetic energy of |k| >= 20",
+                       "checkpoint_every": every, "fd_h": h, "directions": 8},
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "mixed_gradient_rel_l2_vs_fp64": math.sqrt(num / den),
+            "mixed_J_rel_vs_fp64": abs(res["mixed"]["J"] - res["fp64"]["J"]) / abs(res["fp64"]["J"])}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,14 +608,28 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer timing (profiling runs)")
-    ap.add_argument("--size", type=int, default=512, help="grid size (default 512; smaller only for ncu)")
+    ap.add_argument("--size", type=int, default=512,
+                    help="grid size (512 default; 1024 runs the roofline sweep's second size with nu = 8e-5)")
+    ap.add_argument("--workload", default="roofline", choices=["roofline", "precision", "ensemble", "adjoint"],
+                    help="roofline: the headline 512^3 step (default); precision: 256^3 2D2C FP64 vs mixed; "
+                         "ensemble: 64 uneven members, graph launch; adjoint: 128^3 gradient checks")
     args = ap.parse_args()
     global N
+    global METRIC
     N = args.size
+    METRIC = METRIC_FMT.format(n=N)
+    if N >= 1024:
+        PHYS["nu"] = 8e-5
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "precision":
+        return run_precision(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_ours(args)
 
 

@@ -4,10 +4,10 @@ The compute path is ``libgturbo_gb.so`` (hand-written CUDA, C-ABI in
 ``include/gturbo_gb.h``); this package is its Python binding and the
 seeded synthetic-input generator.
 """
-from .api import (Simulation, ForcedModes, forced_modes, forcing_amplitude, forcing_increments,
-                  make_params,
-                  rann, read_field, read_params, read_seed, write_field, write_seed)
+from .api import (Ensemble, Simulation, ForcedModes, autotune, forced_modes, forcing_amplitude,
+                  forcing_increments, make_params, rann, read_field, read_params, read_seed, write_field,
+                  write_seed)
 
-__all__ = ["Simulation", "ForcedModes", "forced_modes", "forcing_amplitude", "forcing_increments",
-           "make_params", "rann",
+__all__ = ["Ensemble", "Simulation", "ForcedModes", "autotune", "forced_modes", "forcing_amplitude",
+           "forcing_increments", "make_params", "rann",
            "read_field", "read_params", "read_seed", "write_field", "write_seed"]
