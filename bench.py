@@ -369,6 +369,14 @@ def run_ours(args):
             rel_err = abs(e32 - e64) / e64
         sim64.close()
 
+    # --- FP64 issue rates: the plain form's roofline denominators ------------
+    alu = None
+    if args.fp64_steps > 0:
+        try:
+            alu = __import__("gturbo3d_gb300").probe_alu(device)
+        except Exception as ex:   # the probe is a report, not the measurement
+            alu = {"error": str(ex)[:200]}
+
     # --- roofline of the dominant kernel --------------------------------------
     peaks = measured_peaks()
     hbm = peaks["hbm_gbs"] if peaks else 6800.0
@@ -401,7 +409,8 @@ def run_ours(args):
             "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps},
+            "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps,
+                     "bound": "fp64 alu (DADD/DFMA issue; HBM is not the limit)", "alu_probe_ginst_s": alu},
             "rel_energy_err_mixed_vs_fp64": rel_err, "energy_steps": args.energy_steps,
             "roofline": roof, "clocks": clk}
     sim.close()

@@ -81,6 +81,8 @@ SIGNATURES = {
     "gt_set_pruning": (C.c_int, [_vp, C.c_int32]),
     "gt_pruning_active": (C.c_int, [_vp, _ip]),
     "gt_set_pipelining": (C.c_int, [_vp, C.c_int32]),
+    "gt_selftest_wait_timeout": (C.c_int, [_vp]),
+    "gt_probe_alu": (C.c_int, [C.c_int32, _dp]),
     "gt_set_tuning": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "gt_autotune": (C.c_int, [_vp, C.c_char_p, _dp]),
     "gt_tl_step": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),

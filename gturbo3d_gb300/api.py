@@ -59,6 +59,14 @@ def read_params(path: str, base: GtParams | None = None) -> GtParams:
     return p
 
 
+def probe_alu(device: int = 0) -> dict:
+    """This GPU's ALU issue rates (gt_probe_alu), G thread-instructions/s."""
+    lib = load()
+    r = np.zeros(4)
+    check(lib.gt_probe_alu(int(device), _dp(r)), "gt_probe_alu")
+    return {"dfma": float(r[0]), "dadd": float(r[1]), "ffma": float(r[2]), "fadd": float(r[3])}
+
+
 def rann(seed: int, n: int) -> tuple[np.ndarray, int]:
     """n draws of the reference RNG from state ``seed``; returns (values, seed)."""
     lib = load()
@@ -254,6 +262,11 @@ class Simulation:
 
     def check_finite(self) -> int:
         return self.lib.gt_check_finite(self.h)
+
+    def selftest_wait_timeout(self) -> int:
+        """Runs the bounded-wait self-test; returns its status (GT_ETIMEOUT = -7
+        when the wait ran out as it should)."""
+        return self.lib.gt_selftest_wait_timeout(self.h)
 
     def set_pipelining(self, enable: bool) -> None:
         check(self.lib.gt_set_pipelining(self.h, 1 if enable else 0), "gt_set_pipelining")

@@ -769,6 +769,14 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   return GT_OK;
 }
 
+int gt_selftest_wait_timeout(gt_handle* h) {
+  if (!h) return GT_EINVAL;
+  int rc = set_dev(h);
+  if (rc) return rc;
+  if ((rc = launch_wait_selftest(h->d_err, h->stream))) return cuda_fail((cudaError_t)rc, "launch_wait_selftest");
+  return check_device_flag(h);
+}
+
 int gt_set_pipelining(gt_handle* h, int32_t enable) {
   if (!h) return GT_EINVAL;
   h->use_pipe = enable != 0;

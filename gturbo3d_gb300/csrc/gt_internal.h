@@ -148,6 +148,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
 int zpass_default_tx(const Geom& g, int csize);
 int ypipe_tx(const Geom& g, int csize);
 int zpipe_tx(const Geom& g, int csize);
+int launch_wait_selftest(int* err, void* stream);
 template <typename R>
 int launch_xpipe(const Geom& g, void* const w[6], const void* twx, int xa, int pairs, int nstage,
                  int* err, void* stream, LaunchHook hook, void* hctx);

@@ -641,6 +641,27 @@ int launch_ypipe(const Geom& g, const PipeMaps& pm, void* const* fields, int nf,
   return (int)cudaGetLastError();
 }
 
+// Self-test of the bounded-wait path: one thread waits on an mbarrier that
+// nothing arrives at (no copy is issued), gives up after `limit` polls and
+// records GT_ETIMEOUT in the error flag, exactly as a pipelined pass does when
+// its copies never land.  Nothing is in flight when it returns.
+__global__ void k_wait_selftest(int* err, uint32_t limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    bool ok = false;
+    for (uint32_t i = 0; i < limit && !ok; ++i) ok = mbar_try_wait(&bar, 0);
+    if (!ok) raise_error(err, GT_ETIMEOUT);
+    mbar_inval(&bar);
+  }
+}
+
+int launch_wait_selftest(int* err, void* stream) {
+  k_wait_selftest<<<1, 32, 0, (cudaStream_t)stream>>>(err, 1u << 12);
+  return (int)cudaGetLastError();
+}
+
 template int launch_ypipe<float>(const Geom&, const PipeMaps&, void* const*, int, const void*, int, int,
                                  int, const int32_t*, int*, void*, LaunchHook, void*);
 template int launch_ypipe<double>(const Geom&, const PipeMaps&, void* const*, int, const void*, int, int,

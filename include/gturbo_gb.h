@@ -261,6 +261,18 @@ int gt_ensemble_energy(gt_ensemble* e, double* energy);
 /* gt_autotune once per distinct (grid, precision) class, applied to all its members. */
 int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path);
 
+/* Exercises the bounded-wait failure path of the pipelined passes without a
+ * fault: a kernel waits on an mbarrier that nothing completes, gives up after a
+ * few thousand polls and sets the handle's error flag.  Returns GT_ETIMEOUT
+ * (and clears the flag); the handle stays usable.  No reference counterpart. */
+int gt_selftest_wait_timeout(gt_handle* h);
+
+/* Measures this GPU's ALU issue rates in G thread-instructions per second:
+ * rates[0] DFMA, [1] DADD, [2] FFMA, [3] FADD (independent chains, 8 blocks of
+ * 256 threads per SM).  The FP64 form of the step is FP64-ALU bound; these are
+ * its roofline denominators.  No reference counterpart. */
+int gt_probe_alu(int32_t device, double* rates);
+
 /* ---- introspection ------------------------------------------------------- */
 const char* gt_strerror(int code);
 /* Text of the last CUDA failure seen on the calling thread ("" if none). */

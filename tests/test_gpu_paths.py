@@ -34,3 +34,20 @@ def test_initial_state_path(lib, precision, tol):
         got = sim.get_state()
     assert relerr(got, ref) < tol
     assert abs(cc - cc_ref) / cc_ref < max(tol, 1e-12) * 10
+
+
+@pytest.mark.gpu
+def test_bounded_wait_times_out_and_handle_survives(lib):
+    """A device wait that nothing completes gives up, reports GT_ETIMEOUT
+    through the error flag, and the handle keeps stepping correctly."""
+    import gturbo3d_gb300 as g
+    gp, _ = configs(16, forcing="none")
+    b0 = initial(16, seed=2)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        b.set_state(b0)
+        assert a.selftest_wait_timeout() == -7
+        assert a.selftest_wait_timeout() == -7        # the flag was cleared and set again
+        a.step(2, 0)
+        b.step(2, 0)
+        assert relerr(a.get_state(), b.get_state()) == 0.0
