@@ -765,6 +765,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
   else if (k == "x_fused") h->pm.x_fused = value != 0;
+  else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else return GT_EINVAL;
   return GT_OK;
 }

@@ -28,6 +28,43 @@ template <typename R> using Cplx = typename CplxOf<R>::type;
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
 
+// FP32 complex add/sub as one paired instruction (add.rn.f32x2 / sub.rn.f32x2,
+// sm_100 and later): each lane is rounded to nearest as two add.rn.f32 would
+// be, so results are bit-identical and the butterflies issue half the adds.
+#ifndef GT_NO_F32X2
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+#endif
+
+// Two complex values of adjacent x columns, transformed together by one
+// thread of a strided pass (a 16-byte load or store for FP32): the twiddle
+// and the index arithmetic of a stage serve both.
+template <typename R> struct __align__(2 * sizeof(Cplx<R>)) CPair {
+  Cplx<R> a, b;
+};
+template <typename R> __device__ __forceinline__ CPair<R> cadd(CPair<R> p, CPair<R> q) {
+  return CPair<R>{cadd(p.a, q.a), cadd(p.b, q.b)};
+}
+template <typename R> __device__ __forceinline__ CPair<R> csub(CPair<R> p, CPair<R> q) {
+  return CPair<R>{csub(p.a, q.a), csub(p.b, q.b)};
+}
+
 // a * W4^{SIGN}: the forward transform multiplies by -i, the inverse by +i.
 template <int SIGN, typename C> __device__ __forceinline__ C rot90(C a) {
   return SIGN < 0 ? C{a.y, -a.x} : C{-a.y, a.x};
@@ -37,6 +74,13 @@ template <int SIGN, typename C> __device__ __forceinline__ C rot90(C a) {
 template <int SIGN, typename C> __device__ __forceinline__ C twmul(C a, C w) {
   if (SIGN < 0) return C{a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x};
   return C{a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y};
+}
+
+template <int SIGN, typename R> __device__ __forceinline__ CPair<R> rot90(CPair<R> p) {
+  return CPair<R>{rot90<SIGN>(p.a), rot90<SIGN>(p.b)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CPair<R> twmul(CPair<R> p, Cplx<R> w) {
+  return CPair<R>{twmul<SIGN>(p.a, w), twmul<SIGN>(p.b, w)};
 }
 
 template <typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
@@ -54,27 +98,47 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft4(C& x0, C& x
   x3 = csub(d0, d1);
 }
 
+// Multiplication by W8 = (1 -+ i)/sqrt2 and W8^3 = (-1 -+ i)/sqrt2 (upper sign
+// forward), and the radix-2 combination e +- o of such a product written
+// component-wise so that the products fuse into FMAs.
+template <int SIGN, typename R> __device__ __forceinline__ Cplx<R> w8_1(Cplx<R> o) {
+  const R c = (R)0.70710678118654752440;
+  return SIGN < 0 ? Cplx<R>{c * (o.x + o.y), c * (o.y - o.x)} : Cplx<R>{c * (o.x - o.y), c * (o.x + o.y)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ Cplx<R> w8_3(Cplx<R> o) {
+  const R c = (R)0.70710678118654752440;
+  return SIGN < 0 ? Cplx<R>{c * (o.y - o.x), -c * (o.x + o.y)} : Cplx<R>{-c * (o.x + o.y), c * (o.x - o.y)};
+}
+template <typename C> __device__ __forceinline__ C fadd(C e, C o) { return C{e.x + o.x, e.y + o.y}; }
+template <typename C> __device__ __forceinline__ C fsub(C e, C o) { return C{e.x - o.x, e.y - o.y}; }
+template <int SIGN, typename R> __device__ __forceinline__ CPair<R> w8_1(CPair<R> p) {
+  return CPair<R>{w8_1<SIGN, R>(p.a), w8_1<SIGN, R>(p.b)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CPair<R> w8_3(CPair<R> p) {
+  return CPair<R>{w8_3<SIGN, R>(p.a), w8_3<SIGN, R>(p.b)};
+}
+template <typename R> __device__ __forceinline__ CPair<R> fadd(CPair<R> e, CPair<R> o) {
+  return CPair<R>{fadd(e.a, o.a), fadd(e.b, o.b)};
+}
+template <typename R> __device__ __forceinline__ CPair<R> fsub(CPair<R> e, CPair<R> o) {
+  return CPair<R>{fsub(e.a, o.a), fsub(e.b, o.b)};
+}
+
 // 8-point DFT in natural order: two 4-point DFTs of the even and odd inputs,
-// the odd outputs rotated by W8^q, then one radix-2 layer.
+// the odd outputs rotated by W8^q, then one radix-2 layer.  C is a complex
+// value or a CPair of two.
 template <int SIGN, typename R, typename C> __device__ __forceinline__ void dft8(C v[8]) {
   C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
   C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
   dft4<SIGN>(e0, e1, e2, e3);
   dft4<SIGN>(o0, o1, o2, o3);
-  const R c = (R)0.70710678118654752440;
-  if (SIGN < 0) {  // W8 = (1 - i)/sqrt2, W8^3 = (-1 - i)/sqrt2
-    o1 = C{c * (o1.x + o1.y), c * (o1.y - o1.x)};
-    o2 = C{o2.y, -o2.x};
-    o3 = C{c * (o3.y - o3.x), -c * (o3.x + o3.y)};
-  } else {         // W8 = (1 + i)/sqrt2, W8^3 = (-1 + i)/sqrt2
-    o1 = C{c * (o1.x - o1.y), c * (o1.x + o1.y)};
-    o2 = C{-o2.y, o2.x};
-    o3 = C{-c * (o3.x + o3.y), c * (o3.x - o3.y)};
-  }
+  o1 = w8_1<SIGN, R>(o1);
+  o2 = rot90<SIGN>(o2);
+  o3 = w8_3<SIGN, R>(o3);
   v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
-  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+  v[1] = fadd(e1, o1); v[5] = fsub(e1, o1);
   v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
-  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+  v[3] = fadd(e3, o3); v[7] = fsub(e3, o3);
 }
 
 // Shared-memory addressing of one line.
@@ -181,9 +245,9 @@ constexpr int tw_stage_offset(int lgl, int lgns) {
 // left at run time.  Twiddles come from the per-stage table stored after the
 // L entries of the full table (`tw + L`), where the lanes of a warp read
 // consecutive entries.
-template <int SIGN, typename R, int LGL, int LGNS, typename Idx, typename Sync>
-__device__ __forceinline__ void fft_stages_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw,
-                                              Cplx<R>* sm, const Idx& idx, const Sync& sync) {
+template <int SIGN, typename R, int LGL, int LGNS, typename E, typename Idx, typename Sync>
+__device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
+                                              const Idx& idx, const Sync& sync) {
   using C = Cplx<R>;
   constexpr int REM = LGL - LGNS;
   constexpr int LR = REM >= 3 ? 3 : REM;
@@ -255,8 +319,10 @@ struct NamedSync {
   }
 };
 
-template <int SIGN, typename R, int LGL, typename Idx, typename Sync = BlockSync>
-__device__ __forceinline__ void fft_line_ct(Cplx<R> v[8], int t, const Cplx<R>* __restrict__ tw, Cplx<R>* sm,
+// E is the element a thread holds per position: Cplx<R>, or CPair<R> for two
+// adjacent columns sharing the stage's twiddles.
+template <int SIGN, typename R, int LGL, typename E, typename Idx, typename Sync = BlockSync>
+__device__ __forceinline__ void fft_line_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
                                             const Idx& idx, const Sync& sync = Sync{}) {
   fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx, sync);
 }

@@ -112,6 +112,7 @@ struct PipeMaps {
   int pipe_y = 0, pipe_z = 0, pipe_x = 0;
   int x_pairs = 1, x_stages = 2;
   int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
+  int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
   int x_fused = 1;          // x pass: 1 = one thread group per row pair (cross product in
                             // registers), 0 = three groups per row pair
 };

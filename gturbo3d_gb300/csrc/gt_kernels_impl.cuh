@@ -67,47 +67,101 @@ static int ilog2i(int n) {
 // Block: (L/8) x TX threads; thread (t, x) owns positions z = t + i L/8 of
 // column X = tile*TX + x.  Shared memory: three [nz][TX] regions.
 // ---------------------------------------------------------------------------
+// W columns per thread (1, or 2 for FP32: 16-byte accesses, twiddles and
+// index arithmetic shared); E holds one position of those columns.
+template <typename R, int W> struct ColVec { using type = Cplx<R>; };
+template <typename R> struct ColVec<R, 2> { using type = CPair<R>; };
+template <typename R, int W> using ColT = typename ColVec<R, W>::type;
+
+__device__ __forceinline__ float2& col(float2& e, int) { return e; }
+__device__ __forceinline__ double2& col(double2& e, int) { return e; }
+template <typename R> __device__ __forceinline__ Cplx<R>& col(CPair<R>& e, int c) { return c ? e.b : e.a; }
+
+// The W columns X0.. of one position at p[o]; columns >= lim read as zero.
+template <typename R, int W>
+__device__ __forceinline__ ColT<R, W> load_cols(const Cplx<R>* __restrict__ p, size_t o, int X0, int lim) {
+  using C = Cplx<R>;
+  if constexpr (W == 1) {
+    return X0 < lim ? p[o] : C{0, 0};
+  } else {
+    if (X0 + 1 < lim) return *reinterpret_cast<const CPair<R>*>(p + o);
+    return CPair<R>{X0 < lim ? p[o] : C{0, 0}, C{0, 0}};
+  }
+}
+// Stores the columns < lim of one position.
+template <typename R, int W>
+__device__ __forceinline__ void store_cols(Cplx<R>* __restrict__ p, size_t o, int X0, int lim, const ColT<R, W>& v) {
+  if constexpr (W == 1) {
+    if (X0 < lim) p[o] = v;
+  } else {
+    if (X0 + 1 < lim) {
+      *reinterpret_cast<CPair<R>*>(p + o) = v;
+    } else if (X0 < lim) {
+      p[o] = v.a;
+    }
+  }
+}
+
+// Columns per thread of the z inverse pass: 2 for FP32, 1 for FP64.  The z
+// forward pass keeps one column per thread: its epilogue works column by
+// column, and pairs measured slower there (0.49 ms against 0.46 ms at 512^3).
+template <typename R> constexpr int zcols() { return sizeof(R) == 4 ? 2 : 1; }
+template <typename R> constexpr int zfwd_cols() { return 1; }
+
 template <typename R, int LGZ>
-__global__ void __launch_bounds__(max_threads<R>())
+__global__ void __launch_bounds__(max_threads<R>() / zcols<R>())
 k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
   using C = Cplx<R>;
+  constexpr int W = zcols<R>();
+  using E = ColT<R, W>;
   extern __shared__ __align__(16) unsigned char smraw[];
-  C* sm = reinterpret_cast<C*>(smraw);
-  const int TX = 1 << lgTX;
-  const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
   int tile = blockIdx.x, y = blockIdx.y;
   if (pruned) {
     tile = tiles[2 * blockIdx.x];
     y = tiles[2 * blockIdx.x + 1];
   }
-  const int X = tile * TX + x;
-  const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;   // columns with data in this y row
+  const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = strided_rows(1 << LGZ) * TX;
-  C* S0 = sm;
-  C* S1 = sm + reg;
-  C* S2 = sm + 2 * reg;
-  const StridedIdxLg idx{lgTX, x};
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const int reg = strided_rows(1 << LGZ) * TP;
+  E* S0 = sm;
+  E* S1 = sm + reg;
+  E* S2 = sm + 2 * reg;
+  const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   const C* a0 = reinterpret_cast<const C*>(a.p[0]);
   const C* a1 = reinterpret_cast<const C*>(a.p[1]);
   const C* a2 = reinterpret_cast<const C*>(a.p[2]);
-  const R kx = valid ? tb.fkx[X] : (R)0, ky = tb.fky[y];
-  const R kxs = valid ? tb.fkxs[X] : (R)0, kys = tb.fkys[y];
-  C v[8];
+  R kx[W], kxs[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const bool in = X0 + c < ylim;
+    kx[c] = in ? tb.fkx[X0 + c] : (R)0;
+    kxs[c] = in ? tb.fkxs[X0 + c] : (R)0;
+  }
+  const R ky = tb.fky[y], kys = tb.fkys[y];
+  E v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int z = t + i * T;
-    C ux{0, 0}, uy{0, 0}, uz{0, 0};
-    if (valid && (!pruned || X < tb.xcut[(size_t)z * g.ny + y])) {
-      const size_t o = (size_t)z * plane + base;
-      const C ax = a0[o], ay = a1[o], az = a2[o];
-      const R kz = tb.fkz[z];
-      ux = C{-ky * az.y + kz * ay.y, ky * az.x - kz * ay.x};
-      uy = C{-kz * ax.y + kx * az.y, kz * ax.x - kx * az.x};
-      uz = C{-kx * ay.y + ky * ax.y, kx * ay.x - ky * ax.x};
+    const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+    const size_t o = (size_t)z * plane + base;
+    E ax = load_cols<R, W>(a0, o, X0, lim), ay = load_cols<R, W>(a1, o, X0, lim),
+      az = load_cols<R, W>(a2, o, X0, lim);
+    const R kz = tb.fkz[z];
+    E ux, uy, uz;
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const C px = col(ax, c), py = col(ay, c), pz = col(az, c);
+      col(ux, c) = C{-ky * pz.y + kz * py.y, ky * pz.x - kz * py.x};
+      col(uy, c) = C{-kz * px.y + kx[c] * pz.y, kz * px.x - kx[c] * pz.x};
+      col(uz, c) = C{-kx[c] * py.y + ky * px.y, kx[c] * py.x - ky * px.x};
     }
     v[i] = ux;
     S1[idx(z)] = uy;
@@ -115,42 +169,39 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
   }
   C* out0 = reinterpret_cast<C*>(w.p[0]);
   fft_line_ct<+1, R, LGZ>(v, t, tw, S0, idx);
-  if (valid) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) out0[(size_t)(t + i * T) * plane + base] = v[i];
-  }
+  for (int i = 0; i < 8; ++i) store_cols<R, W>(out0, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   for (int f = 1; f < 3; ++f) {
-    C* S = f == 1 ? S1 : S2;
+    E* S = f == 1 ? S1 : S2;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
     __syncthreads();
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
     C* out = reinterpret_cast<C*>(w.at(f));
-    if (valid) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
-    }
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   }
-  for (int c = 0; c < 3; ++c) {
-    const C* ac = reinterpret_cast<const C*>(a.at(c));
+  for (int c3 = 0; c3 < 3; ++c3) {
+    const C* ac = reinterpret_cast<const C*>(a.at(c3));
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int z = t + i * T;
-      C val{0, 0};
-      if (valid && (!pruned || X < tb.xcut[(size_t)z * g.ny + y])) {
-        const R k2 = (kxs + kys) + tb.fkzs[z];
-        const C av = ac[(size_t)z * plane + base];
-        val = C{k2 * av.x, k2 * av.y};
-      }
-      v[i] = val;
-    }
-    C* S = c == 0 ? S0 : (c == 1 ? S1 : S2);
-    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
-    C* out = reinterpret_cast<C*>(w.at(3 + c));
-    if (valid) {
+      const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+      E av = load_cols<R, W>(ac, (size_t)z * plane + base, X0, lim);
+      const R kzs = tb.fkzs[z];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) out[(size_t)(t + i * T) * plane + base] = v[i];
+      for (int c = 0; c < W; ++c) {
+        const R k2 = (kxs[c] + kys) + kzs;
+        const C q = col(av, c);
+        col(av, c) = C{k2 * q.x, k2 * q.y};
+      }
+      v[i] = av;
     }
+    E* S = c3 == 0 ? S0 : (c3 == 1 ? S1 : S2);
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.at(3 + c3));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   }
 }
 
@@ -194,6 +245,56 @@ k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, i
     for (int i = 0; i < 8; ++i) {
       const int e = t + i * T;
       if (ymask != 2 || X < xcut0[e]) p[base + (size_t)e * (size_t)ls] = v[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The strided transform with two adjacent x columns per thread (FP32): one
+// 16-byte load or store per position, the stage twiddles and index
+// arithmetic shared by both columns, twice the bytes in flight per thread.
+// Block: (L/8) x TP threads for a tile of 2 TP columns; the shared tile is
+// [rows][TP] column pairs with the y/z padding rows.  Column X0 = 2 (tile TP
+// + xp); a pair straddling xlim or the pruning cut moves element by element.
+// ---------------------------------------------------------------------------
+template <int SIGN, int LGL>
+__global__ void __launch_bounds__(kSpassThreads, 3)
+k_spass2(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTP, int xlim, int ymask,
+         const int32_t* __restrict__ xcut0) {
+  using C = float2;
+  using E = CPair<float>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  const int X0 = 2 * (blockIdx.x * TP + xp);
+  constexpr int T = 1 << (LGL - 3);
+  C* p = reinterpret_cast<C*>(f.at(blockIdx.z));
+  const size_t base = (size_t)blockIdx.y * (size_t)os + (X0 < xlim ? X0 : 0);
+  const StridedIdxLg idx{lgTP, xp};
+  E v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int e = t + i * T;
+    const int cut = ymask == 1 ? min(xlim, xcut0[e]) : xlim;
+    const C* src = p + base + (size_t)e * (size_t)ls;
+    if (X0 + 1 < cut) {
+      v[i] = *reinterpret_cast<const E*>(src);
+    } else {
+      v[i].a = X0 < cut ? src[0] : C{0, 0};
+      v[i].b = C{0, 0};
+    }
+  }
+  fft_line_ct<SIGN, float, LGL>(v, t, reinterpret_cast<const C*>(twv), sm, idx);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int e = t + i * T;
+    const int cut = ymask == 2 ? min(xlim, xcut0[e]) : xlim;
+    C* dst = p + base + (size_t)e * (size_t)ls;
+    if (X0 + 1 < cut) {
+      *reinterpret_cast<E*>(dst) = v[i];
+    } else if (X0 < cut) {
+      dst[0] = v[i].a;
     }
   }
 }
@@ -406,93 +507,113 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 // Pass 5: forward z transform of three fields, then the spectral epilogue.
 // ---------------------------------------------------------------------------
 template <typename R, int LGZ>
-__global__ void __launch_bounds__(max_threads<R>())
+__global__ void __launch_bounds__(max_threads<R>() / zfwd_cols<R>())
 k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
            const int32_t* __restrict__ tiles) {
   using C = Cplx<R>;
+  constexpr int W = zfwd_cols<R>();
+  using E = ColT<R, W>;
   extern __shared__ __align__(16) unsigned char smraw[];
-  C* sm = reinterpret_cast<C*>(smraw);
-  const int TX = 1 << lgTX;
-  const int x = threadIdx.x & (TX - 1), t = threadIdx.x >> lgTX;
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
   int tile = blockIdx.x, y = blockIdx.y;
   if (pruned) {
     tile = tiles[2 * blockIdx.x];
     y = tiles[2 * blockIdx.x + 1];
   }
-  const int X = tile * TX + x;
-  const bool valid = X < (pruned ? tb.xcut[y] : g.nh);
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X : 0);
-  const int reg = strided_rows(1 << LGZ) * TX;
-  const StridedIdxLg idx{lgTX, x};
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const int reg = strided_rows(1 << LGZ) * TP;
+  const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
-  C v[8];
+  E v[8];
   for (int f = 0; f < 3; ++f) {
     const C* in = reinterpret_cast<const C*>(w.at(f));
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = valid ? in[(size_t)(t + i * T) * plane + base] : C{0, 0};
-    C* S = sm + f * reg;
+    for (int i = 0; i < 8; ++i) v[i] = load_cols<R, W>(in, (size_t)(t + i * T) * plane + base, X0, ylim);
+    E* S = sm + f * reg;
     fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
   }
   if (!valid) return;  // no barrier follows
-  const R kx = tb.fkx[X], ky = tb.fky[y], kxs = tb.fkxs[X], kys = tb.fkys[y];
+  const R ky = tb.fky[y], kys = tb.fkys[y];
   const C* b0p = reinterpret_cast<const C*>(bc.p[0]);
   const C* b1p = reinterpret_cast<const C*>(bc.p[1]);
   const C* b2p = reinterpret_cast<const C*>(bc.p[2]);
   C* o0 = reinterpret_cast<C*>(out.p[0]);
   C* o1 = reinterpret_cast<C*>(out.p[1]);
   C* o2 = reinterpret_cast<C*>(out.p[2]);
-  const int* xcut = tb.xcut + (size_t)0;
 #pragma unroll 2
   for (int i = 0; i < 8; ++i) {
     const int z = t + i * T;
-    const bool kept = X < xcut[(size_t)z * g.ny + y];
-    if (pruned && !kept) continue;   // zero outside K in both the state and the result
+    const int zlim = tb.xcut[(size_t)z * g.ny + y];      // kept modes of this row: X < zlim
+    // columns whose result is written: all of the row's columns, or only the
+    // kept ones when pruned (zero outside K in both the state and the result)
+    const int wlim = pruned ? zlim : ylim;
+    if (X0 >= wlim) continue;
     const size_t o = (size_t)z * plane + base;
-    const C n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
-    const C b0 = b0p[o], b1 = b1p[o], b2 = b2p[o];
-    // nlt.f90:67-81: a = v + i omega kz b(t)
-    const R okz = tb.omega * tb.fkz[z];
-    const C a0{n0.x - okz * b0.y, n0.y + okz * b0.x};
-    const C a1{n1.x - okz * b1.y, n1.y + okz * b1.x};
-    const C a2{n2.x - okz * b2.y, n2.y + okz * b2.x};
-    const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
-    const R k2 = (kxs + kys) + tb.fkzs[z];
-    C r0 = a0, r1 = a1, r2 = a2;
-    if (!zero_mode) {  // produ.f90:83-99: i k x a / k^2
-      const R ik2 = (R)1 / k2;
-      const R qx = kx * ik2, qy = ky * ik2, qz = tb.fkz[z] * ik2;
-      r0 = C{-qy * a2.y + qz * a1.y, qy * a2.x - qz * a1.x};
-      r1 = C{-qz * a0.y + qx * a2.y, qz * a0.x - qx * a2.x};
-      r2 = C{-qx * a1.y + qy * a0.y, qx * a1.x - qy * a0.x};
-    }
-    if (tb.truncate && (zero_mode || !kept)) {  // trunc.f90:14-28
-      r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
-    }
-    if (mode == kNltOnly) {
-      o0[o] = r0; o1[o] = r1; o2[o] = r2;
-    } else {
-      const R e = tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X];
-      C s0, s1, s2;
-      if (mode == kStage1) {  // rkstep.f90:126-135: c = emk (a + dt2 c)
-        const R d = tb.dt2;
-        s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
-        s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
-        s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};
-      } else {                // rkstep.f90:182-191: a = emk (emk a + dt c)
-        const R d = tb.dt;
-        s0 = C{e * (e * b0.x + d * r0.x), e * (e * b0.y + d * r0.y)};
-        s1 = C{e * (e * b1.x + d * r1.x), e * (e * b1.y + d * r1.y)};
-        s2 = C{e * (e * b2.x + d * r2.x), e * (e * b2.y + d * r2.y)};
+    E n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
+    E bb0 = load_cols<R, W>(b0p, o, X0, wlim), bb1 = load_cols<R, W>(b1p, o, X0, wlim),
+      bb2 = load_cols<R, W>(b2p, o, X0, wlim);
+    const R kz = tb.fkz[z], kzs = tb.fkzs[z];
+    const R okz = tb.omega * kz;
+    E res0, res1, res2;
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const int X = X0 + c;
+      const C b0 = col(bb0, c), b1 = col(bb1, c), b2 = col(bb2, c);
+      const C m0 = col(n0, c), m1 = col(n1, c), m2 = col(n2, c);
+      // nlt.f90:67-81: a = v + i omega kz b(t)
+      const C a0{m0.x - okz * b0.y, m0.y + okz * b0.x};
+      const C a1{m1.x - okz * b1.y, m1.y + okz * b1.x};
+      const C a2{m2.x - okz * b2.y, m2.y + okz * b2.x};
+      const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
+      const bool kept = X < zlim;
+      const R kxv = X < g.nh ? tb.fkx[X] : (R)0, kxsv = X < g.nh ? tb.fkxs[X] : (R)0;
+      const R k2 = (kxsv + kys) + kzs;
+      C r0 = a0, r1 = a1, r2 = a2;
+      if (!zero_mode) {  // produ.f90:83-99: i k x a / k^2
+        const R ik2 = (R)1 / k2;
+        const R qx = kxv * ik2, qy = ky * ik2, qz = kz * ik2;
+        r0 = C{-qy * a2.y + qz * a1.y, qy * a2.x - qz * a1.x};
+        r1 = C{-qz * a0.y + qx * a2.y, qz * a0.x - qx * a2.x};
+        r2 = C{-qx * a1.y + qy * a0.y, qx * a1.x - qy * a0.x};
       }
-      if (zero_mode) {        // rkstep.f90:140-144 / 196-200
-        s0 = C{0, 0}; s1 = C{0, 0}; s2 = C{0, 0};
+      if (tb.truncate && (zero_mode || !kept)) {  // trunc.f90:14-28
+        r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
       }
-      o0[o] = s0; o1[o] = s1; o2[o] = s2;
+      if (mode == kNltOnly) {
+        col(res0, c) = r0; col(res1, c) = r1; col(res2, c) = r2;
+      } else {
+        const R e = X >= g.nh ? (R)0
+                    : (tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X]);
+        C s0, s1, s2;
+        if (mode == kStage1) {  // rkstep.f90:126-135: c = emk (a + dt2 c)
+          const R d = tb.dt2;
+          s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
+          s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
+          s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};
+        } else {                // rkstep.f90:182-191: a = emk (emk a + dt c)
+          const R d = tb.dt;
+          s0 = C{e * (e * b0.x + d * r0.x), e * (e * b0.y + d * r0.y)};
+          s1 = C{e * (e * b1.x + d * r1.x), e * (e * b1.y + d * r1.y)};
+          s2 = C{e * (e * b2.x + d * r2.x), e * (e * b2.y + d * r2.y)};
+        }
+        if (zero_mode) {        // rkstep.f90:140-144 / 196-200
+          s0 = C{0, 0}; s1 = C{0, 0}; s2 = C{0, 0};
+        }
+        col(res0, c) = s0; col(res1, c) = s1; col(res2, c) = s2;
+      }
     }
+    store_cols<R, W>(o0, o, X0, wlim, res0);
+    store_cols<R, W>(o1, o, X0, wlim, res1);
+    store_cols<R, W>(o2, o, X0, wlim, res2);
   }
 }
 
@@ -924,12 +1045,16 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 7 + 1];
+  cudaError_t es[8 * 9 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
   es[n++] = allow_smem(k_spass<R, 1, LG>, optin);        \
   es[n++] = allow_smem(k_spass<R, -1, LG>, optin);       \
+  if (sizeof(R) == 4) {                                  \
+    es[n++] = allow_smem(k_spass2<1, LG>, optin);        \
+    es[n++] = allow_smem(k_spass2<-1, LG>, optin);       \
+  }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
   es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
@@ -963,7 +1088,7 @@ static int set_smem_attrs() {
 template <typename R>
 static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int axis, int sign,
                  cudaStream_t s, LaunchHook hook, void* hctx, int xlim = -1, int ymask = 0,
-                 const int32_t* xcut0 = nullptr, int force_tx = 0) {
+                 const int32_t* xcut0 = nullptr, int force_tx = 0, bool pairs = false) {
   const int csize = sizeof(Cplx<R>);
   const int L = axis == 1 ? g.ny : g.nz;
   const int lgL = axis == 1 ? g.lny : g.lnz;
@@ -978,6 +1103,26 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
   for (int i = 0; i < nf; ++i) f.p[i] = fields[i];
   const int ntx = (xlim + TX - 1) / TX;
   const int kind = sign > 0 ? kKYPass : kKYFwd;
+  if (pairs) {
+    // FP32, two columns per thread: the tile is chosen for 2 x kSpassThreads
+    // threads of one column each, then halved
+    SCfg c2 = strided_cfg(L, g.nh, 1, csize, 2 * kSpassThreads, force_tx);
+    if (c2.lgTX >= 1) {
+      const int TX2 = 1 << c2.lgTX;
+      const int ntx2 = (xlim + TX2 - 1) / TX2;
+      dim3 grid2(ntx2, outer, nf);
+      GT_HOOK(kind, true);
+#define GT_L(LG)                                                                                      \
+  if (sign > 0)                                                                                       \
+    k_spass2<1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0); \
+  else                                                                                                \
+    k_spass2<-1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0);
+      GT_DISPATCH_LG(lgL, GT_L)
+#undef GT_L
+      GT_HOOK(kind, false);
+      return (int)cudaGetLastError();
+    }
+  }
   dim3 grid(ntx, outer, nf);
   GT_HOOK(kind, true);
 #define GT_L(LG)                                                                                  \
@@ -1003,13 +1148,16 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
   // pass 1
   {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
+    if (c.lgTX < zcols<R>() - 1) return (int)cudaErrorInvalidConfiguration;   // a column pair per thread
     if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;   // no tile list
     Ptr6 pa{}, pw{};
     for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
-#define GT_L(LG) k_zinv_curl<R, LG><<<grid, c.threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
+#define GT_L(LG)                                                                                   \
+  k_zinv_curl<R, LG><<<grid, c.threads / zcols<R>(), c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned,    \
+                                                                  tb.ztl[c.lgTX]);
     GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     GT_HOOK(kKZinvCurl, false);
@@ -1017,14 +1165,17 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
   }
   const int xlim = pruned ? tb.xa : g.nh;
   // y passes: 32-byte tile rows for FP32 by default (measured best at 512^3)
-  const int ytx = pm && pm->y_tx ? pm->y_tx : (sizeof(R) == 4 ? 4 : 0);
+  // FP32 y passes with two columns per thread unless switched off; tile
+  // columns: 8 with column pairs, 4 without (measured best at 512^3)
+  const bool ypairs = sizeof(R) == 4 && (!pm || pm->y_pairs);
+  const int ytx = pm && pm->y_tx ? pm->y_tx : (sizeof(R) == 4 ? (ypairs ? 8 : 4) : 0);
   // pass 2
   if (pm && pm->valid && pm->pipe_y) {
     if ((rc = launch_ypipe<R>(g, *pm, w, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
                               hook, hctx)))
       return rc;
   } else if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
-                            ytx))) {
+                            ytx, ypairs))) {
     return rc;
   }
   // pass 3
@@ -1073,7 +1224,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
                               hook, hctx)))
       return rc;
   } else if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
-                            ytx))) {
+                            ytx, ypairs))) {
     return rc;
   }
   // pass 5
@@ -1082,6 +1233,7 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
       return rc;
   } else {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
+    if (c.lgTX < zfwd_cols<R>() - 1) return (int)cudaErrorInvalidConfiguration;
     if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;
     Ptr6 pw{}, pb{}, po{};
     for (int i = 0; i < 3; ++i) {
@@ -1091,7 +1243,9 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     }
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZFwdEpi, true);
-#define GT_L(LG) k_zfwd_epi<R, LG><<<grid, c.threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned, tb.ztl[c.lgTX]);
+#define GT_L(LG)                                                                                   \
+  k_zfwd_epi<R, LG><<<grid, c.threads / zfwd_cols<R>(), c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, \
+                                                                 pruned, tb.ztl[c.lgTX]);
     GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     GT_HOOK(kKZFwdEpi, false);

@@ -94,3 +94,25 @@ def test_fused_x_pass_equals_three_group_pass(lib, n, precision, tol, truncate):
         b.step(3, 5)
         assert relerr(a.get_state(), b.get_state()) < tol
 
+
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [64, (16, 64, 32), (64, 1024, 8), (64, 8, 16), (8, 16, 16), (128, 32, 64)])
+@pytest.mark.parametrize("truncate", [1, 0])
+def test_paired_y_pass_equals_plain(lib, n, truncate):
+    """FP32 y passes with two adjacent columns per thread give the result of
+    the one-column-per-thread y passes (same arithmetic, bit for bit up to
+    the compiler's FMA contraction)."""
+    import gturbo3d_gb300 as g
+    gp, _ = configs(n, precision="mixed", forcing="3d3c", truncate=truncate)
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(n, seed=11)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        b.set_state(b0)
+        a.set_tuning("y_pairs", 1)
+        b.set_tuning("y_pairs", 0)
+        a.step(3, 5)
+        b.step(3, 5)
+        assert relerr(a.get_state(), b.get_state()) < 1e-6
