@@ -245,21 +245,62 @@ constexpr int tw_stage_offset(int lgl, int lgns) {
 // left at run time.  Twiddles come from the per-stage table stored after the
 // L entries of the full table (`tw + L`), where the lanes of a warp read
 // consecutive entries.
+// The twiddles one thread applies in the stage that starts after 2^LGNS
+// points: radix 8: 7 for its butterfly; radix 4: 3 for each of its 2
+// butterflies; radix 2: 1 for each of its 4.  Loaded a stage ahead, so that
+// their latency overlaps the previous stage's butterflies and exchange.
+template <typename R, int LGL, int LGNS> struct StageTw {
+  static constexpr int REM = LGL - LGNS;
+  static constexpr int LR = REM >= 3 ? 3 : REM;
+  static constexpr int NS = 1 << LGNS;
+  static constexpr int T = 1 << (LGL - 3);
+  static constexpr int N = LGNS == 0 ? 1 : (LR == 3 ? 7 : (LR == 2 ? 6 : 4));
+  Cplx<R> w[N];
+  __device__ __forceinline__ void load(int t, const Cplx<R>* __restrict__ tw) {
+    if constexpr (LGNS > 0) {
+      const Cplx<R>* tws = tw + (1 << LGL) + tw_stage_offset(LGL, LGNS);
+      if constexpr (LR == 3) {
+        const int k = t & (NS - 1);
+#pragma unroll
+        for (int j = 1; j < 8; ++j) w[j - 1] = __ldg(&tws[(j - 1) * NS + k]);
+      } else if constexpr (LR == 2) {
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          const int k = (t + m * T) & (NS - 1);
+          w[3 * m] = __ldg(&tws[k]);
+          w[3 * m + 1] = __ldg(&tws[NS + k]);
+          w[3 * m + 2] = __ldg(&tws[2 * NS + k]);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) w[m] = __ldg(&tws[(t + m * T) & (NS - 1)]);
+      }
+    }
+  }
+};
+
 template <int SIGN, typename R, int LGL, int LGNS, typename E, typename Idx, typename Sync>
 __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
-                                              const Idx& idx, const Sync& sync) {
-  using C = Cplx<R>;
+                                              const Idx& idx, const Sync& sync,
+                                              const StageTw<R, LGL, LGNS>& cur) {
   constexpr int REM = LGL - LGNS;
   constexpr int LR = REM >= 3 ? 3 : REM;
   constexpr bool LAST = (REM == LR);
   constexpr int NS = 1 << LGNS;
   constexpr int T = 1 << (LGL - 3);
-  const C* tws = tw + (1 << LGL) + tw_stage_offset(LGL, LGNS);
+  // FP32: twiddles a stage ahead (measured faster); FP64: at the stage
+  // itself (the extra live registers spill in the FP64 z pass)
+  constexpr bool PF = sizeof(R) == 4;
+  StageTw<R, LGL, LGNS + LR> nxt;
+  if constexpr (!LAST && PF) nxt.load(t, tw);
+  StageTw<R, LGL, LGNS> own;
+  if constexpr (!PF) own.load(t, tw);
+  const StageTw<R, LGL, LGNS>& tws = PF ? cur : own;
   if constexpr (LR == 3) {
     const int k = t & (NS - 1);
     if constexpr (LGNS > 0) {
 #pragma unroll
-      for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tws[(j - 1) * NS + k]));
+      for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], tws.w[j - 1]);
     }
     dft8<SIGN, R>(v);
     if constexpr (!LAST) {
@@ -273,9 +314,9 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
       const int b = t + m * T;
       const int k = b & (NS - 1);
       if constexpr (LGNS > 0) {
-        v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tws[k]));
-        v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tws[NS + k]));
-        v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tws[2 * NS + k]));
+        v[m + 2] = twmul<SIGN>(v[m + 2], tws.w[3 * m]);
+        v[m + 4] = twmul<SIGN>(v[m + 4], tws.w[3 * m + 1]);
+        v[m + 6] = twmul<SIGN>(v[m + 6], tws.w[3 * m + 2]);
       }
       dft4<SIGN>(v[m], v[m + 2], v[m + 4], v[m + 6]);
       if constexpr (!LAST) {
@@ -289,7 +330,7 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
     for (int m = 0; m < 4; ++m) {
       const int b = t + m * T;
       const int k = b & (NS - 1);
-      if constexpr (LGNS > 0) v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tws[k]));
+      if constexpr (LGNS > 0) v[m + 4] = twmul<SIGN>(v[m + 4], tws.w[m]);
       dft2(v[m], v[m + 4]);
       if constexpr (!LAST) {
         const int base = ((b >> LGNS) << (LGNS + 1)) + k;
@@ -303,7 +344,7 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
     sync();
-    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx, sync);
+    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx, sync, nxt);
   }
 }
 
@@ -324,7 +365,8 @@ struct NamedSync {
 template <int SIGN, typename R, int LGL, typename E, typename Idx, typename Sync = BlockSync>
 __device__ __forceinline__ void fft_line_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
                                             const Idx& idx, const Sync& sync = Sync{}) {
-  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx, sync);
+  const StageTw<R, LGL, 0> none{};
+  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx, sync, none);
 }
 
 // Strided shared-memory tile of a y or z pass: element e of column x of a

@@ -1169,64 +1169,67 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
   // columns: 8 with column pairs, 4 without (measured best at 512^3)
   const bool ypairs = sizeof(R) == 4 && (!pm || pm->y_pairs);
   const int ytx = pm && pm->y_tx ? pm->y_tx : (sizeof(R) == 4 ? (ypairs ? 8 : 4) : 0);
-  // pass 2
-  if (pm && pm->valid && pm->pipe_y) {
-    if ((rc = launch_ypipe<R>(g, *pm, w, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
-                              hook, hctx)))
-      return rc;
-  } else if ((rc = spass<R>(g, w, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
-                            ytx, ypairs))) {
-    return rc;
-  }
-  // pass 3
-  if (pm && pm->valid && pm->pipe_x) {
-    if ((rc = launch_xpipe<R>(g, w, tb.twx, xlim, pm->x_pairs, pm->x_stages, err, stream, hook, hctx)))
-      return rc;
-  } else if (!pm || pm->x_fused) {
-    // one group of nx/8 threads per row pair; as many groups per block as fit
-    // in xfused_threads and divide the number of row pairs
-    const int T = g.nx / 8;
-    const long long npairs = (long long)g.ny * g.nz / 2;
-    int P = 1;
-    while (P * 2 * T <= xfused_threads<R>() && npairs % (P * 2) == 0) P <<= 1;
-    if (P * T > xfused_threads<R>() || npairs % P != 0) return (int)cudaErrorInvalidConfiguration;
-    const int LP = g.nx;
-    const int smem = P * LP * csize;
-    Ptr6 pw{};
-    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
-    const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
-    GT_HOOK(kKXCross, true);
-#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, g, tb.twx, shalf, xlim);
-    GT_DISPATCH_LG(g.lnx, GT_L)
+  const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
+  // passes 2-4 (the y and x passes; gs and ws are the grid and work fields)
+  auto middle = [&](const Geom& gs, void* const* ws) -> int {
+    int rc2 = 0;
+    // pass 2
+    if (pm && pm->valid && pm->pipe_y) {
+      if ((rc2 = launch_ypipe<R>(gs, *pm, ws, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
+                                 hook, hctx)))
+        return rc2;
+    } else if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
+                               ytx, ypairs))) {
+      return rc2;
+    }
+    // pass 3
+    if (pm && pm->valid && pm->pipe_x) {
+      if ((rc2 = launch_xpipe<R>(gs, ws, tb.twx, xlim, pm->x_pairs, pm->x_stages, err, stream, hook, hctx)))
+        return rc2;
+    } else if (!pm || pm->x_fused) {
+      // one group of nx/8 threads per row pair; as many groups per block as
+      // fit in xfused_threads and divide the number of row pairs
+      const int T = gs.nx / 8;
+      const long long npairs = (long long)gs.ny * gs.nz / 2;
+      int P = 1;
+      while (P * 2 * T <= xfused_threads<R>() && npairs % (P * 2) == 0) P <<= 1;
+      if (P * T > xfused_threads<R>() || npairs % P != 0) return (int)cudaErrorInvalidConfiguration;
+      const int smem = P * gs.nx * csize;
+      Ptr6 pw{};
+      for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
+      GT_HOOK(kKXCross, true);
+#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+      GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
-    GT_HOOK(kKXCross, false);
-    if ((rc = (int)cudaGetLastError())) return rc;
-  } else {
-    const int P = xpass_pairs(g, 3, csize, max_threads<R>(), 6);
-    const int threads = 3 * P * (g.nx / 8);
-    if (threads > (g.lnx >= 10 ? 384 : 192)) return (int)cudaErrorInvalidConfiguration;
-    const int LP = g.nx;
-    const int smem = 6 * P * LP * csize;
-    const long long nblocks = (long long)g.ny * g.nz / 2 / P;
-    Ptr6 pw{};
-    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
-    const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
-    GT_HOOK(kKXCross, true);
-#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, g, tb.twx, P, shalf, xlim);
-    GT_DISPATCH_LG(g.lnx, GT_L)
+      GT_HOOK(kKXCross, false);
+      if ((rc2 = (int)cudaGetLastError())) return rc2;
+    } else {
+      const int P = xpass_pairs(gs, 3, csize, max_threads<R>(), 6);
+      const int threads = 3 * P * (gs.nx / 8);
+      if (threads > (gs.lnx >= 10 ? 384 : 192)) return (int)cudaErrorInvalidConfiguration;
+      const int smem = 6 * P * gs.nx * csize;
+      const long long nblocks = (long long)gs.ny * gs.nz / 2 / P;
+      Ptr6 pw{};
+      for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
+      GT_HOOK(kKXCross, true);
+#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, gs, tb.twx, P, shalf, xlim);
+      GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
-    GT_HOOK(kKXCross, false);
-    if ((rc = (int)cudaGetLastError())) return rc;
-  }
-  // pass 4
-  if (pm && pm->valid && pm->pipe_y) {
-    if ((rc = launch_ypipe<R>(g, *pm, w, 3, tb.twy, -1, xlim, pruned ? 2 : 0, tb.xcut, err, stream,
-                              hook, hctx)))
-      return rc;
-  } else if ((rc = spass<R>(g, w, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
-                            ytx, ypairs))) {
-    return rc;
-  }
+      GT_HOOK(kKXCross, false);
+      if ((rc2 = (int)cudaGetLastError())) return rc2;
+    }
+    // pass 4
+    if (pm && pm->valid && pm->pipe_y) {
+      if ((rc2 = launch_ypipe<R>(gs, *pm, ws, 3, tb.twy, -1, xlim, pruned ? 2 : 0, tb.xcut, err, stream,
+                                 hook, hctx)))
+        return rc2;
+    } else if ((rc2 = spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
+                               ytx, ypairs))) {
+      return rc2;
+    }
+    return 0;
+  };
+  if ((rc = middle(g, w))) return rc;
   // pass 5
   if (pm && pm->valid && pm->pipe_z && pm->ztx > 0) {
     if ((rc = launch_zpipe_epi<R>(g, tb, *pm, bcor, out, mode, pruned, err, stream, hook, hctx)))

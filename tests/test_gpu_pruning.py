@@ -116,3 +116,4 @@ def test_paired_y_pass_equals_plain(lib, n, truncate):
         a.step(3, 5)
         b.step(3, 5)
         assert relerr(a.get_state(), b.get_state()) < 1e-6
+
