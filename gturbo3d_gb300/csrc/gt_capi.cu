@@ -864,12 +864,12 @@ const char* gt_last_error(void) { return g_last_error.c_str(); }
 namespace {
 
 struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused;
+  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs;
 };
 
 Tuning get_tuning(const gt_handle* h) {
   return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
-                h->pm.z_tx, h->pm.x_fused};
+                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs};
 }
 
 void put_tuning(gt_handle* h, const Tuning& t) {
@@ -881,6 +881,7 @@ void put_tuning(gt_handle* h, const Tuning& t) {
   h->pm.y_tx = t.y_tx;
   h->pm.z_tx = t.z_tx;
   h->pm.x_fused = t.x_fused;
+  h->pm.y_pairs = t.y_pairs;
 }
 
 std::string tuning_key(const gt_handle* h) {
@@ -911,7 +912,8 @@ bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
     };
     if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
         get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
-        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused)) {
+        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
+        get("\"y_pairs\": ", u.y_pairs)) {
       t = u;
       found = true;   // the last matching line wins
     }
@@ -927,8 +929,9 @@ void cache_store(const char* path, const std::string& key, const Tuning& t, doub
   std::fprintf(f,
                "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
                "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
-               "\"ms_per_step\": %.6f}\n",
-               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused, ms);
+               "\"y_pairs\": %d, \"ms_per_step\": %.6f}\n",
+               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused,
+               t.y_pairs, ms);
   std::fclose(f);
 }
 
@@ -985,7 +988,8 @@ int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
   const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
                                    {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
                                    {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
-                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1}}};
+                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1}},
+                                   {&Tuning::y_pairs, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {
       if (best.*(k.field) == v) continue;

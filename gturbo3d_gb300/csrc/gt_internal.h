@@ -146,7 +146,6 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
                void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
                int* err, void* stream, LaunchHook hook, void* hctx);
 // Default tile width of the plain z passes (3 fields in shared memory).
-int zpass_default_tx(const Geom& g, int csize);
 int ypipe_tx(const Geom& g, int csize);
 int zpipe_tx(const Geom& g, int csize);
 int launch_wait_selftest(int* err, void* stream);

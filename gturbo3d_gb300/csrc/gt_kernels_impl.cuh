@@ -1423,10 +1423,6 @@ int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], doubl
 }
 
 #ifdef GT_KERNELS_COMMON
-int zpass_default_tx(const Geom& g, int csize) {
-  return 1 << strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024).lgTX;
-}
-
 void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles, int tx) {
   const SCfg c = strided_cfg(g.nz, g.nh, 3, csize, csize == 16 ? 512 : 1024);
   const int TX = tx > 0 ? tx : 1 << c.lgTX;
