@@ -381,7 +381,7 @@ def autotune(sim: "Simulation", cache_path: str | None = None) -> float:
 
 class Ensemble:
     """Independent members advanced together (gt_ensemble_*): in graph mode one
-    captured CUDA graph launch per step advances every member."""
+    captured CUDA graph launch advances every member by 64 steps."""
 
     def __init__(self, params: list):
         self.lib = load()

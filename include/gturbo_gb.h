@@ -252,10 +252,11 @@ int gt_ensemble_set_state(gt_ensemble* e, int32_t member, const double* bx, cons
                           const double* bz);
 int gt_ensemble_get_state(gt_ensemble* e, int32_t member, double* bx, double* by, double* bz);
 /* nsteps RK2 steps of every member; seeds[n] are the members' forcing seeds
- * (advanced).  graph = 1: one captured CUDA graph launch per step advances
- * all members (member kernels run concurrently on their own streams);
- * graph = 0: the same kernels launched member by member.  The forcing is
- * drawn on the host in chunks of 64 steps. */
+ * (advanced).  The forcing is drawn on the host in chunks of 64 steps.
+ * graph = 1: one captured CUDA graph launch per chunk advances every member
+ * by 64 steps (each member's kernels on its own stream, joined at the end of
+ * the chunk; a shorter last chunk is launched directly); graph = 0: the same
+ * kernels launched member by member and step by step. */
 int gt_ensemble_step(gt_ensemble* e, int32_t nsteps, int32_t* seeds, int32_t graph);
 /* Total kinetic energy of each member (n values). */
 int gt_ensemble_energy(gt_ensemble* e, double* energy);
