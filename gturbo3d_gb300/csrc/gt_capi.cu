@@ -672,11 +672,12 @@ int gt_energy(gt_handle* h, double* energy_xyz) {
   int rc = set_dev(h);
   if (rc) return rc;
   const int nblk = diag_blocks(h->g);
+  const int pr = use_pruning(h) ? 1 : 0;   // state zero outside the kept set
   if (h->mixed)
-    CKI(launch_energy<float>(h->g, h->t32, h->b, h->d_partials, nblk, h->d_result, h->stream,
+    CKI(launch_energy<float>(h->g, h->t32, h->b, pr, h->d_partials, nblk, h->d_result, h->stream,
                              hook_fn, h));
   else
-    CKI(launch_energy<double>(h->g, h->t64, h->b, h->d_partials, nblk, h->d_result, h->stream,
+    CKI(launch_energy<double>(h->g, h->t64, h->b, pr, h->d_partials, nblk, h->d_result, h->stream,
                               hook_fn, h));
   CK(cudaMemcpyAsync(h->h_result, h->d_result, 3 * sizeof(double), cudaMemcpyDeviceToHost,
                      h->stream));

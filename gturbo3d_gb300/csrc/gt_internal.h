@@ -201,7 +201,7 @@ int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* c
                 double* result /* kDiagScalars + 3*nbin */, void* stream, LaunchHook hook,
                 void* hctx);
 template <typename R>
-int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], double* partials,
+int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], int pruned, double* partials,
                   int nblocks, double* result, void* stream, LaunchHook hook, void* hctx);
 int diag_blocks(const Geom& g);
 // Tangent-linear / adjoint building blocks (gt_adjoint.cu): out = op(a) [+ beta b].

@@ -926,7 +926,7 @@ k_diag(Ptr6 bb, Ptr6 nn, DevTables<R> tb, Geom g, double nu, double alpnu, doubl
 // products in the working precision, accumulation and reduction in FP64.
 template <typename R>
 __global__ void __launch_bounds__(kDiagThreads)
-k_energy(Ptr6 bb, DevTables<R> tb, Geom g, double* partials) {
+k_energy(Ptr6 bb, DevTables<R> tb, Geom g, int pruned, double* partials) {
   using C = Cplx<R>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double e0 = 0.0, e1 = 0.0, e2 = 0.0;
@@ -935,7 +935,10 @@ k_energy(Ptr6 bb, DevTables<R> tb, Geom g, double* partials) {
   for (size_t row = (size_t)blockIdx.x * 8 + warp; row < rows; row += nwarps) {
     const int y = (int)(row % g.ny), z = (int)(row / g.ny);
     const R ky = tb.fky[y], kz = tb.fkz[z];
-    for (int X = lane; X < g.nh; X += 32) {
+    // pruned: the state is zero outside the kept prefix of the row, whose
+    // terms would add exact zeros to the same partial sums
+    const int xend = pruned ? tb.xcut[row] : g.nh;
+    for (int X = lane; X < xend; X += 32) {
       const size_t o = row * g.nhp + X;
       const C b0 = reinterpret_cast<const C*>(bb.p[0])[o];
       const C b1 = reinterpret_cast<const C*>(bb.p[1])[o];
@@ -1407,12 +1410,12 @@ int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* c
 }
 
 template <typename R>
-int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], double* partials,
+int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], int pruned, double* partials,
                   int nblocks, double* result, void* stream, LaunchHook hook, void* hctx) {
   Ptr6 pb{};
   for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
   GT_HOOK(kKDiag, true);
-  k_energy<R><<<nblocks, kDiagThreads, 0, (cudaStream_t)stream>>>(pb, tb, g, partials);
+  k_energy<R><<<nblocks, kDiagThreads, 0, (cudaStream_t)stream>>>(pb, tb, g, pruned, partials);
   GT_HOOK(kKDiag, false);
   int rc = (int)cudaGetLastError();
   if (rc) return rc;
@@ -1493,7 +1496,7 @@ const char* kernel_kind_name(int k) {
                                  void* const*, void*, LaunchHook, void*);                       \
   template int launch_point<R>(const Geom&, const DevTables<R>&, void* const*, int, double*,   \
                                int, void*, LaunchHook, void*);                                  \
-  template int launch_energy<R>(const Geom&, const DevTables<R>&, void* const*, double*, int,  \
+  template int launch_energy<R>(const Geom&, const DevTables<R>&, void* const*, int, double*, int, \
                                 double*, void*, LaunchHook, void*);                             \
   template int launch_diag<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,    \
                               double, double, double, double, double*, int, double*, void*,    \

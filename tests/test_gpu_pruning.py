@@ -117,3 +117,21 @@ def test_paired_y_pass_equals_plain(lib, n, truncate):
         b.step(3, 5)
         assert relerr(a.get_state(), b.get_state()) < 1e-6
 
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pruned_energy_reduction_is_exact(lib, precision):
+    """The energy reduction that visits only the kept modes (state zero
+    outside them) gives the full reduction bit for bit."""
+    import gturbo3d_gb300 as g
+    gp, _ = configs((32, 64, 16), precision=precision, forcing="3d3c")
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    with g.Simulation(gp) as sim:
+        sim.set_state(initial((32, 64, 16), seed=13))
+        sim.step(2, 5)
+        assert sim.pruning_active
+        e_pruned = sim.energy()
+        sim.set_pruning(False)
+        assert not sim.pruning_active
+        assert sim.energy() == e_pruned
