@@ -288,14 +288,33 @@ void free_handle(gt_handle* h) {
 }
 
 // ---- dispatch on precision ----------------------------------------------
+// The launch-shape state for one call: the tuning knobs always apply; the
+// TMA-pipelined variants only while pipelining is on and their tensor maps
+// exist.
+PipeMaps effective_tuning(const gt_handle* h) {
+  PipeMaps pm = h->pm;
+  if (!h->use_pipe || !pm.valid) pm.pipe_y = pm.pipe_z = pm.pipe_x = 0;
+  return pm;
+}
+
 int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
         int pruned = 0) {
-  const PipeMaps* pm = (h->use_pipe && h->pm.valid) ? &h->pm : nullptr;
+  const PipeMaps pm = effective_tuning(h);
   if (h->mixed)
-    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, pm, h->d_err, h->stream,
+    return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, &pm, h->d_err, h->stream,
                              hook_fn, h);
-  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, pruned, pm, h->d_err, h->stream,
+  return launch_nlt<double>(h->g, h->t64, a, bcor, out, h->w, mode, pruned, &pm, h->d_err, h->stream,
                             hook_fn, h);
+}
+
+// Both nonlinear terms of one RK2 step, b -> c -> b (main.f90:124-146).
+int rk2_nlts(gt_handle* h, int pruned) {
+  const PipeMaps pm = effective_tuning(h);
+  if (h->mixed)
+    return launch_rk2_nlts<float>(h->g, h->t32, h->b, h->c, h->w, pruned, &pm, h->d_err, h->stream,
+                                  hook_fn, h);
+  return launch_rk2_nlts<double>(h->g, h->t64, h->b, h->c, h->w, pruned, &pm, h->d_err, h->stream,
+                                 hook_fn, h);
 }
 
 // Reads (and clears) the device error flag of the bounded waits.
@@ -442,8 +461,7 @@ int run_steps(gt_handle* h, int nsteps, const std::vector<ForceEntry>& all,
   }
   const int pr = use_pruning(h) ? 1 : 0;
   for (int s = 0; s < nsteps; ++s) {
-    CKI(nlt(h, h->b, h->b, h->c, kStage1, pr));   // main.f90:124-141
-    CKI(nlt(h, h->c, h->b, h->b, kStage2, pr));   // main.f90:144-146
+    CKI(rk2_nlts(h, pr));                      // main.f90:124-146
     if (dent) {                               // main.f90:149
       const size_t n = offs[s + 1] - offs[s];
       const bool serial = !entries_unique(all.data() + offs[s], n);
@@ -768,6 +786,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
   else if (k == "x_fused") h->pm.x_fused = value != 0;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
+  else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else return GT_EINVAL;
   return GT_OK;
 }
@@ -866,12 +885,12 @@ const char* gt_last_error(void) { return g_last_error.c_str(); }
 namespace {
 
 struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs;
+  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs, fuse_stage;
 };
 
 Tuning get_tuning(const gt_handle* h) {
   return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
-                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs};
+                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs, h->pm.fuse_stage};
 }
 
 void put_tuning(gt_handle* h, const Tuning& t) {
@@ -884,6 +903,7 @@ void put_tuning(gt_handle* h, const Tuning& t) {
   h->pm.z_tx = t.z_tx;
   h->pm.x_fused = t.x_fused;
   h->pm.y_pairs = t.y_pairs;
+  h->pm.fuse_stage = t.fuse_stage;
 }
 
 std::string tuning_key(const gt_handle* h) {
@@ -915,7 +935,7 @@ bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
     if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
         get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
         get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
-        get("\"y_pairs\": ", u.y_pairs)) {
+        get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage)) {
       t = u;
       found = true;   // the last matching line wins
     }
@@ -931,9 +951,9 @@ void cache_store(const char* path, const std::string& key, const Tuning& t, doub
   std::fprintf(f,
                "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
                "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
-               "\"y_pairs\": %d, \"ms_per_step\": %.6f}\n",
+               "\"y_pairs\": %d, \"fuse_stage\": %d, \"ms_per_step\": %.6f}\n",
                key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused,
-               t.y_pairs, ms);
+               t.y_pairs, t.fuse_stage, ms);
   std::fclose(f);
 }
 
@@ -994,7 +1014,7 @@ int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
                                    {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
                                    {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
                                    {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1}},
-                                   {&Tuning::y_pairs, {0, 1}}};
+                                   {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {
       if (best.*(k.field) == v) continue;
@@ -1405,8 +1425,7 @@ void free_ensemble(gt_ensemble* e) {
 int member_enqueue(gt_ensemble* e, int i) {
   gt_handle* h = e->m[i];
   const int pr = use_pruning(h) ? 1 : 0;
-  CKI(nlt(h, h->b, h->b, h->c, kStage1, pr));
-  CKI(nlt(h, h->c, h->b, h->b, kStage2, pr));
+  CKI(rk2_nlts(h, pr));
   if (e->n_ent[i] > 0) {
     if (h->mixed)
       CKI(launch_force_indexed<float>(h->g, h->b, e->d_ent[i], e->n_ent[i], e->d_step + i, h->stream,

@@ -113,7 +113,8 @@ struct PipeMaps {
   int x_pairs = 1, x_stages = 2;
   int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
   int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
-  int x_fused = 1;          // x pass: 1 = one thread group per row pair (cross product in
+  int x_fused = 1;
+  int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary          // x pass: 1 = one thread group per row pair (cross product in
                             // registers), 0 = three groups per row pair
 };
 using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -137,10 +138,14 @@ using LaunchHook = void (*)(void* ctx, int kind, bool begin);
 
 enum KernelKind {
   kKZinvCurl = 0, kKYPass, kKXCross, kKZFwdEpi, kKForce, kKConvert, kKDiag, kKDiagFinal,
-  kKFft1, kKPoint, kKYFwd, kNumKinds
+  kKFft1, kKPoint, kKYFwd, kKZFwdZinv, kNumKinds
 };
 const char* kernel_kind_name(int k);
 
+template <typename R>
+int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
+                    void* const w[6], int pruned, const PipeMaps* pm, int* err, void* stream,
+                    LaunchHook hook, void* hctx);
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
                void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,

@@ -618,6 +618,144 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 }
 
 // ---------------------------------------------------------------------------
+// Passes 5 and 1 of the RK2 step fused at the stage boundary: the forward z
+// transform of the first nonlinear term and its stage-1 epilogue give
+// c = emk (b + dt2 N1) (rkstep.f90:126-144), which stays in shared memory
+// (regions 0-2, written in place of the transformed N1 at each thread's own
+// positions); the inverse z transforms of u = curl c and w = k^2 c for the
+// second nonlinear term (nlt.f90:26-40, produ.f90:44-63) follow, with region
+// 3 as their scratch.  c is never written to or read back from HBM.  One
+// column per thread; the same tiles and pruning as the two separate passes.
+// ---------------------------------------------------------------------------
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(max_threads<R>() / 2 / zcols<R>())
+k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+  using C = Cplx<R>;
+  constexpr int W = zcols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
+  }
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const int reg = strided_rows(1 << LGZ) * TP;
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  E v[8];
+  // forward z transforms of N1 (three fields) into regions 0-2
+  for (int f = 0; f < 3; ++f) {
+    const C* in = reinterpret_cast<const C*>(w.at(f));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = load_cols<R, W>(in, (size_t)(t + i * T) * plane + base, X0, ylim);
+    E* S = sm + f * reg;
+    fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+  }
+  // stage-1 epilogue at this thread's own positions: c in place of N1, zero
+  // where the separate epilogue would not write
+  R kx[W], kxs[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const bool in = X0 + c < ylim;
+    kx[c] = in ? tb.fkx[X0 + c] : (R)0;
+    kxs[c] = in ? tb.fkxs[X0 + c] : (R)0;
+  }
+  const R ky = tb.fky[y], kys = tb.fkys[y];
+  const C* b0p = reinterpret_cast<const C*>(bc.p[0]);
+  const C* b1p = reinterpret_cast<const C*>(bc.p[1]);
+  const C* b2p = reinterpret_cast<const C*>(bc.p[2]);
+#pragma unroll 2
+  for (int i = 0; i < 8; ++i) {
+    const int z = t + i * T;
+    const int zlim = tb.xcut[(size_t)z * g.ny + y];
+    const int wlim = pruned ? zlim : ylim;   // columns the separate epilogue writes
+    const size_t o = (size_t)z * plane + base;
+    E n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
+    E bb0 = load_cols<R, W>(b0p, o, X0, wlim), bb1 = load_cols<R, W>(b1p, o, X0, wlim),
+      bb2 = load_cols<R, W>(b2p, o, X0, wlim);
+    const R kz = tb.fkz[z], kzs = tb.fkzs[z];
+    const R okz = tb.omega * kz;   // nlt.f90:67-81
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const int X = X0 + c;
+      const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
+      C s0{0, 0}, s1{0, 0}, s2{0, 0};
+      if (X < wlim && !zero_mode) {           // rkstep.f90:140-144: c(0) = 0
+        const C b0 = col(bb0, c), b1 = col(bb1, c), b2 = col(bb2, c);
+        const C m0 = col(n0, c), m1 = col(n1, c), m2 = col(n2, c);
+        const C a0{m0.x - okz * b0.y, m0.y + okz * b0.x};
+        const C a1{m1.x - okz * b1.y, m1.y + okz * b1.x};
+        const C a2{m2.x - okz * b2.y, m2.y + okz * b2.x};
+        const R k2 = (kxs[c] + kys) + kzs;
+        const R ik2 = (R)1 / k2;               // produ.f90:83-99
+        const R qx = kx[c] * ik2, qy = ky * ik2, qz = kz * ik2;
+        C r0{-qy * a2.y + qz * a1.y, qy * a2.x - qz * a1.x};
+        C r1{-qz * a0.y + qx * a2.y, qz * a0.x - qx * a2.x};
+        C r2{-qx * a1.y + qy * a0.y, qx * a1.x - qy * a0.x};
+        if (tb.truncate && X >= zlim) {        // trunc.f90:14-28
+          r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
+        }
+        const R e = tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X];
+        const R d = tb.dt2;                    // rkstep.f90:126-135
+        s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
+        s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
+        s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};
+      }
+      col(n0, c) = s0;
+      col(n1, c) = s1;
+      col(n2, c) = s2;
+    }
+    sm[idx(z)] = n0;
+    sm[reg + idx(z)] = n1;
+    sm[2 * reg + idx(z)] = n2;
+  }
+  // inverse z transforms of u = curl c and w = k^2 c from this thread's own
+  // positions of c, with region 3 as scratch
+  E* S3 = sm + 3 * reg;
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      const R kz = tb.fkz[z];
+      E q0 = sm[idx(z)], q1 = sm[reg + idx(z)], q2 = sm[2 * reg + idx(z)];
+      E r;
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const C p0 = col(q0, c), p1 = col(q1, c), p2 = col(q2, c);
+        if (f == 0) {
+          col(r, c) = C{-ky * p2.y + kz * p1.y, ky * p2.x - kz * p1.x};
+        } else if (f == 1) {
+          col(r, c) = C{-kz * p0.y + kx[c] * p2.y, kz * p0.x - kx[c] * p2.x};
+        } else if (f == 2) {
+          col(r, c) = C{-kx[c] * p1.y + ky * p0.y, kx[c] * p1.x - ky * p0.x};
+        } else {
+          const R k2 = (kxs[c] + kys) + tb.fkzs[z];
+          const C q = f == 3 ? p0 : (f == 4 ? p1 : p2);
+          col(r, c) = C{k2 * q.x, k2 * q.y};
+        }
+      }
+      v[i] = r;
+    }
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S3, idx);
+    C* out = reinterpret_cast<C*>(w.at(f));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Plain x transforms (rows of one field packed in pairs).
 // ---------------------------------------------------------------------------
 template <typename R, int LGN>
@@ -1048,7 +1186,7 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 9 + 1];
+  cudaError_t es[8 * 10 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
@@ -1060,6 +1198,7 @@ static int set_smem_attrs() {
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
+  es[n++] = allow_smem(k_zfwd_zinv<R, LG>, optin);       \
   es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
   es[n++] = allow_smem(k_xr2c<R, LG>, optin);
   GT_ALLOW(3) GT_ALLOW(4) GT_ALLOW(5) GT_ALLOW(6) GT_ALLOW(7) GT_ALLOW(8) GT_ALLOW(9) GT_ALLOW(10)
@@ -1140,16 +1279,19 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
 }
 
 template <typename R>
-int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
-               int* err, void* stream, LaunchHook hook, void* hctx) {
+// The passes of one nonlinear term; `phases` selects pass 1 (bit 0), passes
+// 2-4 (bit 1) and pass 5 (bit 2), so that the RK2 step can run the stage
+// boundary as one fused kernel in between.
+static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
+                      void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+                      int* err, void* stream, LaunchHook hook, void* hctx, int phases) {
   int rc = set_smem_attrs<R>();
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
   const int ztx = pm ? pm->z_tx : 0;
   // pass 1
-  {
+  if (phases & 1) {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
     if (c.lgTX < zcols<R>() - 1) return (int)cudaErrorInvalidConfiguration;   // a column pair per thread
     if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;   // no tile list
@@ -1232,9 +1374,10 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     }
     return 0;
   };
-  if ((rc = middle(g, w))) return rc;
+  if ((phases & 2) && (rc = middle(g, w))) return rc;
   // pass 5
-  if (pm && pm->valid && pm->pipe_z && pm->ztx > 0) {
+  if (!(phases & 4)) {
+  } else if (pm && pm->valid && pm->pipe_z && pm->ztx > 0) {
     if ((rc = launch_zpipe_epi<R>(g, tb, *pm, bcor, out, mode, pruned, err, stream, hook, hctx)))
       return rc;
   } else {
@@ -1258,6 +1401,53 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
     if ((rc = (int)cudaGetLastError())) return rc;
   }
   return 0;
+}
+
+template <typename R>
+int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
+               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+               int* err, void* stream, LaunchHook hook, void* hctx) {
+  return nlt_phases<R>(g, tb, a, bcor, out, w, mode, pruned, pm, err, stream, hook, hctx, 7);
+}
+
+// Both nonlinear terms of one RK2 step (main.f90:124-146): b -> c -> b.  With
+// fuse_stage the first term's pass 5 and the second term's pass 1 run as the
+// fused k_zfwd_zinv (c stays on chip; four shared regions per tile, which
+// lowers occupancy: slower than the two passes at 512^3, 1.19 against 1.05 ms);
+// otherwise, and with the TMA-pipelined z pass, c goes through HBM.
+template <typename R>
+int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
+                    void* const w[6], int pruned, const PipeMaps* pm, int* err, void* stream,
+                    LaunchHook hook, void* hctx) {
+  const bool fuse = pm && pm->fuse_stage && !(pm->valid && pm->pipe_z);
+  if (!fuse) {
+    int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 7);
+    if (rc) return rc;
+    return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 7);
+  }
+  int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 1 | 2);
+  if (rc) return rc;
+  {
+    const int csize = sizeof(Cplx<R>);
+    cudaStream_t s = (cudaStream_t)stream;
+    // four regions per tile; 8 columns (FP32, as column pairs) / 2 (FP64) by default
+    SCfg cf = strided_cfg(g.nz, g.nh, 4, csize, max_threads<R>() / 2 * zcols<R>(),
+                          pm && pm->z_tx ? pm->z_tx : (sizeof(R) == 4 ? 8 : 2));
+    if (cf.lgTX < zcols<R>() - 1 || cf.lgTX > 10) return (int)cudaErrorInvalidConfiguration;
+    Ptr6 pw{}, pb{};
+    for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
+    for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+    const dim3 grid = pruned ? dim3(tb.nztl[cf.lgTX]) : dim3(cf.ntiles, g.ny);
+    GT_HOOK(kKZFwdZinv, true);
+#define GT_L(LG)                                                                                  \
+  k_zfwd_zinv<R, LG><<<grid, cf.threads / zcols<R>(), cf.smem, s>>>(pw, pb, tb, g, cf.lgTX, pruned, \
+                                                                   tb.ztl[cf.lgTX]);
+    GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    GT_HOOK(kKZFwdZinv, false);
+    if ((rc = (int)cudaGetLastError())) return rc;
+  }
+  return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 2 | 4);
 }
 
 template <typename R>
@@ -1473,7 +1663,7 @@ int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3]
 const char* kernel_kind_name(int k) {
   static const char* names[kNumKinds] = {"zinv_curl", "yinv", "xcross", "zfwd_epilogue",
                                          "force", "convert", "diag", "diag_final",
-                                         "xc2r_xr2c", "pointwise", "yfwd"};
+                                         "xc2r_xr2c", "pointwise", "yfwd", "zfwd_zinv"};
   return (k >= 0 && k < kNumKinds) ? names[k] : "?";
 }
 #endif
@@ -1482,6 +1672,9 @@ const char* kernel_kind_name(int k) {
   template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
                              void* const*, void* const*, int, int, const PipeMaps*, int*,      \
                              void*, LaunchHook, void*);                                         \
+  template int launch_rk2_nlts<R>(const Geom&, const DevTables<R>&, void* const*, void* const*, \
+                                  void* const*, int, const PipeMaps*, int*, void*, LaunchHook,  \
+                                  void*);                                                      \
   template int launch_count_outside<R>(const Geom&, const DevTables<R>&, void* const*,         \
                                        unsigned long long*, void*);                            \
   template int launch_force<R>(const Geom&, void* const*, const ForceEntry*, int, int, void*,  \

@@ -189,7 +189,9 @@ int gt_set_pipelining(gt_handle* h, int32_t enable);
  * "x_pairs" (row pairs per pipelined x-pass block, 1..8), "x_stages" (2..4),
  * "x_fused" (0/1: x pass with one thread group per row pair and u x w formed in
  * registers, or three groups per row pair), "y_pairs" (0/1: FP32 y passes with
- * two adjacent columns per thread, or one). */
+ * two adjacent columns per thread, or one), "fuse_stage" (0/1: the first nonlinear
+ * term's z forward pass and the second term's z inverse pass as one kernel that
+ * keeps the stage value c on chip, or two passes with c in HBM). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 
 /* Allocation-free kinetic energy, for callers that cannot allocate device

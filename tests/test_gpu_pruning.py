@@ -135,3 +135,25 @@ def test_pruned_energy_reduction_is_exact(lib, precision):
         sim.set_pruning(False)
         assert not sim.pruning_active
         assert sim.energy() == e_pruned
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,precision,tol", [(32, "fp64", 1e-13), (64, "mixed", 1e-5), ((16, 64, 32), "fp64", 1e-13),
+                                             ((64, 32, 16), "mixed", 1e-5), ((8, 16, 1024), "fp64", 1e-13)])
+@pytest.mark.parametrize("truncate,dt2", [(1, "rk2"), (0, "rk2"), (1, "as_built")])
+def test_fused_stage_boundary_equals_separate_passes(lib, n, precision, tol, truncate, dt2):
+    """The RK2 step with the first term's z forward pass and the second
+    term's z inverse pass fused (c kept on chip) equals the step with c
+    written to and read back from HBM."""
+    import gturbo3d_gb300 as g
+    gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate, dt2_mode=dt2)
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(n, seed=14)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        b.set_state(b0)
+        a.set_tuning("fuse_stage", 1)
+        b.set_tuning("fuse_stage", 0)
+        a.step(3, 5)
+        b.step(3, 5)
+        assert relerr(a.get_state(), b.get_state()) < tol
