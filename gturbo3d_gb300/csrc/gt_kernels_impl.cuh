@@ -7,13 +7,15 @@
 //   1. k_zinv_curl  : per (x-tile, y) column block, u = i k x a and w = k^2 a
 //                     formed on load (produ.f90:44-63, nlt.f90:26-40), then
 //                     the inverse z transform of all six fields.
-//   2. k_spass      : inverse y transform of the six fields, in place.
-//   3. k_xcross     : per pair of (y,z) rows, the six C2R x transforms (two
+//   2. k_spass2     : inverse y transform of the six fields, in place (FP32,
+//                     two columns per thread; k_spass for FP64).
+//   3. k_xfused     : per pair of (y,z) rows, the six C2R x transforms (two
 //                     fields per complex FFT), u x w in registers
 //                     (produ.f90:9-28), the three R2C x transforms and the
 //                     1/(NX NY NZ) scaling (fft_dir.f90:17-25); real space
-//                     never reaches HBM.
-//   4. k_spass      : forward y transform of the three fields.
+//                     never reaches HBM (k_xcross: the same with three
+//                     thread groups per row pair).
+//   4. k_spass2     : forward y transform of the three fields.
 //   5. k_zfwd_epi   : forward z transform, then per mode the Coriolis term
 //                     (nlt.f90:67-81), invcurl (produ.f90:79-101), trunc
 //                     (trunc.f90:10-28) and, in a time step, the
@@ -21,6 +23,8 @@
 //                     step2 (rkstep.f90:86-104), written straight into the
 //                     stage or state buffers.
 //
+// With the 2/3 truncation the passes visit only the modes that can be
+// nonzero (tile lists for the z passes, kx < xa for the y and x passes).
 // Spectral fields are [nz][ny][nhp] complex, x fastest, rows padded to a
 // multiple of 128 bytes; columns nh..nhp-1 are never read or written.
 #include <cstdio>
