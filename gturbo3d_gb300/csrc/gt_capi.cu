@@ -784,7 +784,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "x_stages" && value >= 2 && value <= 4) h->pm.x_stages = value;
   else if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
-  else if (k == "x_fused") h->pm.x_fused = value != 0;
+  else if (k == "x_fused" && value >= 0 && value <= 2) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else return GT_EINVAL;
@@ -1013,7 +1013,7 @@ int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
   const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
                                    {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
                                    {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
-                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1}},
+                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1, 2}},
                                    {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {

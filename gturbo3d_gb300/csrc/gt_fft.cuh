@@ -65,6 +65,20 @@ template <typename R> __device__ __forceinline__ CPair<R> csub(CPair<R> p, CPair
   return CPair<R>{csub(p.a, q.a), csub(p.b, q.b)};
 }
 
+// Three complex values at the same position of three lines transformed
+// together by one thread (the x pass's three packed lines of a row): the
+// stage's twiddles, index arithmetic and barriers serve all three, and the
+// three dependency chains interleave.
+template <typename R> struct CTrip {
+  Cplx<R> a, b, c;
+};
+template <typename R> __device__ __forceinline__ CTrip<R> cadd(CTrip<R> p, CTrip<R> q) {
+  return CTrip<R>{cadd(p.a, q.a), cadd(p.b, q.b), cadd(p.c, q.c)};
+}
+template <typename R> __device__ __forceinline__ CTrip<R> csub(CTrip<R> p, CTrip<R> q) {
+  return CTrip<R>{csub(p.a, q.a), csub(p.b, q.b), csub(p.c, q.c)};
+}
+
 // a * W4^{SIGN}: the forward transform multiplies by -i, the inverse by +i.
 template <int SIGN, typename C> __device__ __forceinline__ C rot90(C a) {
   return SIGN < 0 ? C{a.y, -a.x} : C{-a.y, a.x};
@@ -81,6 +95,12 @@ template <int SIGN, typename R> __device__ __forceinline__ CPair<R> rot90(CPair<
 }
 template <int SIGN, typename R> __device__ __forceinline__ CPair<R> twmul(CPair<R> p, Cplx<R> w) {
   return CPair<R>{twmul<SIGN>(p.a, w), twmul<SIGN>(p.b, w)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CTrip<R> rot90(CTrip<R> p) {
+  return CTrip<R>{rot90<SIGN>(p.a), rot90<SIGN>(p.b), rot90<SIGN>(p.c)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CTrip<R> twmul(CTrip<R> p, Cplx<R> w) {
+  return CTrip<R>{twmul<SIGN>(p.a, w), twmul<SIGN>(p.b, w), twmul<SIGN>(p.c, w)};
 }
 
 template <typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
@@ -122,6 +142,18 @@ template <typename R> __device__ __forceinline__ CPair<R> fadd(CPair<R> e, CPair
 }
 template <typename R> __device__ __forceinline__ CPair<R> fsub(CPair<R> e, CPair<R> o) {
   return CPair<R>{fsub(e.a, o.a), fsub(e.b, o.b)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CTrip<R> w8_1(CTrip<R> p) {
+  return CTrip<R>{w8_1<SIGN, R>(p.a), w8_1<SIGN, R>(p.b), w8_1<SIGN, R>(p.c)};
+}
+template <int SIGN, typename R> __device__ __forceinline__ CTrip<R> w8_3(CTrip<R> p) {
+  return CTrip<R>{w8_3<SIGN, R>(p.a), w8_3<SIGN, R>(p.b), w8_3<SIGN, R>(p.c)};
+}
+template <typename R> __device__ __forceinline__ CTrip<R> fadd(CTrip<R> e, CTrip<R> o) {
+  return CTrip<R>{fadd(e.a, o.a), fadd(e.b, o.b), fadd(e.c, o.c)};
+}
+template <typename R> __device__ __forceinline__ CTrip<R> fsub(CTrip<R> e, CTrip<R> o) {
+  return CTrip<R>{fsub(e.a, o.a), fsub(e.b, o.b), fsub(e.c, o.c)};
 }
 
 // 8-point DFT in natural order: two 4-point DFTs of the even and odd inputs,
@@ -279,10 +311,35 @@ template <typename R, int LGL, int LGNS> struct StageTw {
   }
 };
 
-template <int SIGN, typename R, int LGL, int LGNS, typename E, typename Idx, typename Sync>
-__device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
-                                              const Idx& idx, const Sync& sync,
-                                              const StageTw<R, LGL, LGNS>& cur) {
+// Shared scratch of a line transform: element e (logical position) of an
+// array addressed by an index functor ...
+template <typename E, typename Idx> struct ArrMem {
+  E* sm;
+  Idx idx;
+  __device__ __forceinline__ void st(int e, const E& v) const { sm[idx(e)] = v; }
+  __device__ __forceinline__ E ld(int e) const { return sm[idx(e)]; }
+};
+// ... or of three lines kept as three planes `plane` complex values apart (a
+// CTrip per position, each plane addressed like one line).
+template <typename R, typename Idx> struct TripMem {
+  Cplx<R>* sm;
+  Idx idx;
+  int plane;
+  __device__ __forceinline__ void st(int e, const CTrip<R>& v) const {
+    const int i = idx(e);
+    sm[i] = v.a;
+    sm[i + plane] = v.b;
+    sm[i + 2 * plane] = v.c;
+  }
+  __device__ __forceinline__ CTrip<R> ld(int e) const {
+    const int i = idx(e);
+    return CTrip<R>{sm[i], sm[i + plane], sm[i + 2 * plane]};
+  }
+};
+
+template <int SIGN, typename R, int LGL, int LGNS, typename E, typename Mem, typename Sync>
+__device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, const Mem& mem,
+                                              const Sync& sync, const StageTw<R, LGL, LGNS>& cur) {
   constexpr int REM = LGL - LGNS;
   constexpr int LR = REM >= 3 ? 3 : REM;
   constexpr bool LAST = (REM == LR);
@@ -306,7 +363,7 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
     if constexpr (!LAST) {
       const int base = ((t >> LGNS) << (LGNS + 3)) + k;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) sm[idx(base + j * NS)] = v[j];
+      for (int j = 0; j < 8; ++j) mem.st(base + j * NS, v[j]);
     }
   } else if constexpr (LR == 2) {
 #pragma unroll
@@ -322,7 +379,7 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
       if constexpr (!LAST) {
         const int base = ((b >> LGNS) << (LGNS + 2)) + k;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) sm[idx(base + j * NS)] = v[m + 2 * j];
+        for (int j = 0; j < 4; ++j) mem.st(base + j * NS, v[m + 2 * j]);
       }
     }
   } else {
@@ -334,17 +391,17 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
       dft2(v[m], v[m + 4]);
       if constexpr (!LAST) {
         const int base = ((b >> LGNS) << (LGNS + 1)) + k;
-        sm[idx(base)] = v[m];
-        sm[idx(base + NS)] = v[m + 4];
+        mem.st(base, v[m]);
+        mem.st(base + NS, v[m + 4]);
       }
     }
   }
   if constexpr (!LAST) {
     sync();
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
+    for (int i = 0; i < 8; ++i) v[i] = mem.ld(t + i * T);
     sync();
-    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, sm, idx, sync, nxt);
+    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, mem, sync, nxt);
   }
 }
 
@@ -366,7 +423,14 @@ template <int SIGN, typename R, int LGL, typename E, typename Idx, typename Sync
 __device__ __forceinline__ void fft_line_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
                                             const Idx& idx, const Sync& sync = Sync{}) {
   const StageTw<R, LGL, 0> none{};
-  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, sm, idx, sync, none);
+  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, ArrMem<E, Idx>{sm, idx}, sync, none);
+}
+// The same with an explicit scratch policy (ArrMem, TripMem).
+template <int SIGN, typename R, int LGL, typename E, typename Mem, typename Sync>
+__device__ __forceinline__ void fft_line_mem(E v[8], int t, const Cplx<R>* __restrict__ tw, const Mem& mem,
+                                             const Sync& sync) {
+  const StageTw<R, LGL, 0> none{};
+  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, mem, sync, none);
 }
 
 // Strided shared-memory tile of a y or z pass: element e of column x of a

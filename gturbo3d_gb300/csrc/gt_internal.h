@@ -113,9 +113,10 @@ struct PipeMaps {
   int x_pairs = 1, x_stages = 2;
   int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
   int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
-  int x_fused = 1;
-  int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary          // x pass: 1 = one thread group per row pair (cross product in
-                            // registers), 0 = three groups per row pair
+  int x_fused = 2;          // x pass: 2 = one thread group per row pair, a row's three lines
+                            // transformed together; 1 = the lines one by one; 0 = three
+                            // groups per row pair
+  int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary
 };
 using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                      const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,

@@ -508,6 +508,94 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 }
 
 // ---------------------------------------------------------------------------
+// Pass 3 with the three lines of a row transformed together: one group of N/8
+// threads owns a pair of rows; the three packed inverse lines of a row are one
+// CTrip transform (shared twiddles, index arithmetic and barriers; three
+// interleaved dependency chains), kept as three planes of shared memory.  u x w
+// is formed in registers; c_x + i c_y of row 0 waits in registers until the
+// three forward lines (c_x + i c_y of rows 0 and 1, c_z(row 0) + i c_z(row 1))
+// are one CTrip transform.  3 transform calls per row pair instead of 9.
+// ---------------------------------------------------------------------------
+template <typename R> constexpr int xbatch_threads() { return sizeof(R) == 8 ? 128 : 256; }
+
+template <typename R, int LGN>
+__global__ void __launch_bounds__(xbatch_threads<R>(), 2)
+k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
+  using C = Cplx<R>;
+  using E = CTrip<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int N = 1 << LGN, T = N / 8, LP = N;
+  const int grp = threadIdx.x >> (LGN - 3), t = threadIdx.x & (T - 1);
+  const int P = blockDim.x >> (LGN - 3);
+  const size_t pair = (size_t)blockIdx.x * P + grp;
+  const C* tw = reinterpret_cast<const C*>(twv);
+  const size_t nhp = g.nhp;
+  C* lines = sm + (size_t)grp * 3 * LP;
+  const TripMem<R, SwzIdx> mem{lines, SwzIdx{0}, LP};
+  E v[8];
+  C a0[8];
+  R cz0[8];
+  auto run = [&](auto sync) {
+#pragma unroll 1
+    for (int r = 0; r < 2; ++r) {
+      const size_t row = 2 * pair + r;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = t + i * T;
+        v[i].a = pack_c2r<R>(reinterpret_cast<const C*>(w.p[0]) + row * nhp,
+                             reinterpret_cast<const C*>(w.p[1]) + row * nhp, e, N, xa);
+        v[i].b = pack_c2r<R>(reinterpret_cast<const C*>(w.p[2]) + row * nhp,
+                             reinterpret_cast<const C*>(w.p[3]) + row * nhp, e, N, xa);
+        v[i].c = pack_c2r<R>(reinterpret_cast<const C*>(w.p[4]) + row * nhp,
+                             reinterpret_cast<const C*>(w.p[5]) + row * nhp, e, N, xa);
+      }
+      fft_line_mem<+1, R, LGN>(v, t, tw, mem, sync);
+      // u = (z0.x, z0.y, z1.x), w = (z1.y, z2.x, z2.y) (produ.f90:14-16)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const C z0 = v[i].a, z1 = v[i].b, z2 = v[i].c;
+        const R cx = z0.y * z2.y - z1.x * z2.x;
+        const R cy = z1.x * z1.y - z0.x * z2.y;
+        const R cz = z0.x * z2.x - z0.y * z1.y;
+        if (r == 0) {
+          a0[i] = C{cx, cy};
+          cz0[i] = cz;
+        } else {
+          v[i] = E{a0[i], C{cx, cy}, C{cz0[i], cz}};
+        }
+      }
+    }
+    // forward: planes 0, 1, 2 = c_x + i c_y of rows 0 and 1, c_z(0) + i c_z(1)
+    fft_line_mem<-1, R, LGN>(v, t, tw, mem, sync);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) mem.st(t + i * T, v[i]);
+    sync();
+    const size_t row0 = 2 * pair;
+    C* f0 = reinterpret_cast<C*>(w.p[0]);
+    C* f1 = reinterpret_cast<C*>(w.p[1]);
+    C* f2 = reinterpret_cast<C*>(w.p[2]);
+    for (int k = t; k < xa; k += T) {
+      const int kb = (N - k) & (N - 1);
+      const int ia = swz(k), ib = swz(kb);
+#pragma unroll
+      for (int pl = 0; pl < 3; ++pl) {
+        const C a = lines[pl * LP + ia], b = lines[pl * LP + ib];
+        C* oa = (pl == 2 ? f2 : f0) + (row0 + (pl == 1 ? 1 : 0)) * nhp;
+        C* ob = (pl == 2 ? f2 : f1) + (row0 + (pl == 0 ? 0 : 1)) * nhp;
+        oa[k] = split_r2c<R>(a, b, true, shalf);
+        ob[k] = split_r2c<R>(a, b, false, shalf);
+      }
+    }
+  };
+  if constexpr (T >= 32) {
+    run(NamedSync{1 + grp, T});
+  } else {
+    run(BlockSync{});
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Pass 5: forward z transform of three fields, then the spectral epilogue.
 // ---------------------------------------------------------------------------
 template <typename R, int LGZ>
@@ -1190,7 +1278,7 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 10 + 1];
+  cudaError_t es[8 * 11 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
@@ -1201,6 +1289,7 @@ static int set_smem_attrs() {
     es[n++] = allow_smem(k_spass2<-1, LG>, optin);       \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
+  es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
   es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
   es[n++] = allow_smem(k_zfwd_zinv<R, LG>, optin);       \
   es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
@@ -1347,9 +1436,15 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       Ptr6 pw{};
       for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
       GT_HOOK(kKXCross, true);
-#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim);
-      GT_DISPATCH_LG(gs.lnx, GT_L)
+      if (!pm || pm->x_fused == 2) {
+#define GT_L(LG) k_xbatch<R, LG><<<(unsigned)(npairs / P), P * T, 3 * smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+        GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
+      } else {
+#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+        GT_DISPATCH_LG(gs.lnx, GT_L)
+#undef GT_L
+      }
       GT_HOOK(kKXCross, false);
       if ((rc2 = (int)cudaGetLastError())) return rc2;
     } else {

@@ -187,8 +187,9 @@ int gt_set_pipelining(gt_handle* h, int32_t enable);
  * "y_tx", "z_tx" (0 = default, or 2/4/8/16: x-columns per block of the y / z passes),
  * "pipe_y", "pipe_z", "pipe_x" (0/1: TMA-pipelined persistent pass or one tile per block),
  * "x_pairs" (row pairs per pipelined x-pass block, 1..8), "x_stages" (2..4),
- * "x_fused" (0/1: x pass with one thread group per row pair and u x w formed in
- * registers, or three groups per row pair), "y_pairs" (0/1: FP32 y passes with
+ * "x_fused" (x pass: 2 = one thread group per row pair, the three packed lines
+ * of a row transformed together, u x w in registers (default); 1 = the same
+ * with the lines transformed one by one; 0 = three groups per row pair), "y_pairs" (0/1: FP32 y passes with
  * two adjacent columns per thread, or one), "fuse_stage" (0/1: the first nonlinear
  * term's z forward pass and the second term's z inverse pass as one kernel that
  * keeps the stage value c on chip, or two passes with c in HBM). */

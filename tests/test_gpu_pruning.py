@@ -78,9 +78,11 @@ def test_pipelined_passes_equal_plain(lib, n, precision, tol, truncate):
                                              ((8, 16, 16), "fp64", 1e-13), ((16, 32, 8), "mixed", 1e-5),
                                              ((1024, 8, 8), "mixed", 1e-5), ((1024, 8, 8), "fp64", 1e-13)])
 @pytest.mark.parametrize("truncate", [1, 0])
-def test_fused_x_pass_equals_three_group_pass(lib, n, precision, tol, truncate):
-    """The register-resident x pass (one thread group per row pair) and the
-    three-group x pass compute the same u x w and give the same step."""
+@pytest.mark.parametrize("fused", [1, 2])
+def test_fused_x_pass_equals_three_group_pass(lib, n, precision, tol, truncate, fused):
+    """The register-resident x pass (one thread group per row pair; 2: its
+    three lines per row transformed together) and the three-group x pass
+    compute the same u x w and give the same step."""
     import gturbo3d_gb300 as g
     gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate)
     gp.famp = g.forcing_amplitude(0.1, gp)
@@ -88,7 +90,7 @@ def test_fused_x_pass_equals_three_group_pass(lib, n, precision, tol, truncate):
     with g.Simulation(gp) as a, g.Simulation(gp) as b:
         a.set_state(b0)
         b.set_state(b0)
-        a.set_tuning("x_fused", 1)
+        a.set_tuning("x_fused", fused)
         b.set_tuning("x_fused", 0)
         a.step(3, 5)
         b.step(3, 5)
