@@ -82,7 +82,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -448,7 +448,7 @@ def run_precision(args):
     import gturbo3d_gb300 as g
     from gturbo3d_gb300.synth import initial_potential
     from gturbo3d_gb300.workloads import precision_params
-    n, nsteps, seed = args.size if args.size != 512 else 256, args.steps if args.steps != 20 else 200, 1
+    n, nsteps, seed = args.size if args.size != 512 else 256, args.steps if args.steps != 50 else 200, 1
     b0 = initial_potential(n, n, n, seed)
     res = {}
     for prec in ("fp64", "mixed"):
@@ -494,7 +494,7 @@ def run_ensemble(args):
     import torch
     import gturbo3d_gb300 as g
     from gturbo3d_gb300.workloads import ensemble_members, ensemble_params
-    nsteps = args.steps if args.steps != 20 else 500
+    nsteps = args.steps if args.steps != 50 else 500
     members = ensemble_members()
     params = ensemble_params(members)
     seeds0 = np.array([m["seed"] for m in members], np.int32)
@@ -554,7 +554,7 @@ def run_adjoint(args):
     from gturbo3d_gb300.synth import initial_potential
     from gturbo3d_gb300.workloads import adjoint_params, random_direction, spectral_inner
     n = args.size if args.size != 512 else 128
-    nsteps = args.steps if args.steps != 20 else 200
+    nsteps = args.steps if args.steps != 50 else 200
     seed, every, kmin, h = 3, 20, 20.0, 1e-6
     b0 = initial_potential(n, n, n, seed)
     res = {}
@@ -612,7 +612,7 @@ def run_adjoint(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--energy-steps", type=int, default=100)
