@@ -787,6 +787,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "x_fused" && value >= 0 && value <= 2) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
+  else if (k == "z_split") h->pm.z_split = value != 0;
   else return GT_EINVAL;
   return GT_OK;
 }
@@ -885,12 +886,12 @@ const char* gt_last_error(void) { return g_last_error.c_str(); }
 namespace {
 
 struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs, fuse_stage;
+  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split;
 };
 
 Tuning get_tuning(const gt_handle* h) {
   return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
-                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs, h->pm.fuse_stage};
+                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs, h->pm.fuse_stage, h->pm.z_split};
 }
 
 void put_tuning(gt_handle* h, const Tuning& t) {
@@ -904,6 +905,7 @@ void put_tuning(gt_handle* h, const Tuning& t) {
   h->pm.x_fused = t.x_fused;
   h->pm.y_pairs = t.y_pairs;
   h->pm.fuse_stage = t.fuse_stage;
+  h->pm.z_split = t.z_split;
 }
 
 std::string tuning_key(const gt_handle* h) {
@@ -935,7 +937,8 @@ bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
     if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
         get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
         get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
-        get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage)) {
+        get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage) &&
+        get("\"z_split\": ", u.z_split)) {
       t = u;
       found = true;   // the last matching line wins
     }
@@ -951,9 +954,9 @@ void cache_store(const char* path, const std::string& key, const Tuning& t, doub
   std::fprintf(f,
                "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
                "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
-               "\"y_pairs\": %d, \"fuse_stage\": %d, \"ms_per_step\": %.6f}\n",
+               "\"y_pairs\": %d, \"fuse_stage\": %d, \"z_split\": %d, \"ms_per_step\": %.6f}\n",
                key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused,
-               t.y_pairs, t.fuse_stage, ms);
+               t.y_pairs, t.fuse_stage, t.z_split, ms);
   std::fclose(f);
 }
 
@@ -1014,7 +1017,8 @@ int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
                                    {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
                                    {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
                                    {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1, 2}},
-                                   {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}}};
+                                   {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}},
+                                   {&Tuning::z_split, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {
       if (best.*(k.field) == v) continue;

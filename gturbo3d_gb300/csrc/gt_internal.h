@@ -117,6 +117,7 @@ struct PipeMaps {
                             // transformed together; 1 = the lines one by one; 0 = three
                             // groups per row pair
   int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary
+  int z_split = 0;          // z inverse pass: 1 = curl part and k^2 part in separate kernels
 };
 using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                      const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,

@@ -50,6 +50,8 @@ struct Ptr6 {
 constexpr int kSmemBudget = 200 * 1024;
 
 template <typename R> constexpr int max_threads() { return sizeof(R) == 8 ? 512 : 1024; }
+// Block size bound of the strided single-region passes (y passes, w = k^2 a).
+constexpr int kSpassThreads = 256;
 // x passes: at most 3 x (N/8) x P threads with P row pairs chosen so that the
 // block stays within 256 threads (192 for N <= 512, 384 for N = 1024); the
 // register budget per thread is about 80 (FP32) or 168 (FP64).
@@ -114,7 +116,8 @@ template <typename R> constexpr int zfwd_cols() { return 1; }
 
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>() / zcols<R>())
-k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
+            int k2part) {
   using C = Cplx<R>;
   constexpr int W = zcols<R>();
   using E = ColT<R, W>;
@@ -185,6 +188,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 #pragma unroll
     for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   }
+  if (!k2part) return;   // w = k^2 a by k_zk2 (no barrier follows)
   for (int c3 = 0; c3 < 3; ++c3) {
     const C* ac = reinterpret_cast<const C*>(a.at(c3));
 #pragma unroll
@@ -210,13 +214,68 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 }
 
 // ---------------------------------------------------------------------------
+// Pass 1's w = k^2 a on its own (nlt.f90:26-40): per (x-tile, y) column block
+// of the tile list and field f = blockIdx.y, the scaled field's inverse z
+// transform with one shared region, so that more blocks are resident than in
+// the three-region curl kernel.  Same columns, pruning and output as the
+// k^2 half of k_zinv_curl.
+// ---------------------------------------------------------------------------
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(kSpassThreads, sizeof(R) == 8 ? 2 : 3)
+k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+  using C = Cplx<R>;
+  constexpr int W = zcols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  int tile = blockIdx.x, y = blockIdx.z;
+  if (pruned) {
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
+  }
+  const int f = blockIdx.y;
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const StridedIdxLg idx{lgTP, xp};
+  R kxs[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) kxs[c] = X0 + c < ylim ? tb.fkxs[X0 + c] : (R)0;
+  const R kys = tb.fkys[y];
+  const C* ac = reinterpret_cast<const C*>(a.at(f));
+  E v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int z = t + i * T;
+    const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+    E av = load_cols<R, W>(ac, (size_t)z * plane + base, X0, lim);
+    const R kzs = tb.fkzs[z];
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const R k2 = (kxs[c] + kys) + kzs;
+      const C q = col(av, c);
+      col(av, c) = C{k2 * q.x, k2 * q.y};
+    }
+    v[i] = av;
+  }
+  fft_line_ct<+1, R, LGZ>(v, t, reinterpret_cast<const C*>(tb.twz), sm, idx);
+  C* out = reinterpret_cast<C*>(w.at(3 + f));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+}
+
+// ---------------------------------------------------------------------------
 // Strided (y or z) transform of up to six fields, in place.  blockIdx.z picks
 // the field, blockIdx.y the outer index (z for a y pass, y for a z pass).
 // ---------------------------------------------------------------------------
 // At most 256 threads per block; for FP32 five resident blocks (48
 // registers), which hides more load latency than four blocks of 64 registers
 // (measured at 512^3: inverse y pass 1.04 ms against 1.11 ms).
-constexpr int kSpassThreads = 256;
 template <typename R> constexpr int spass_min_blocks() { return sizeof(R) == 8 ? 2 : 5; }
 
 template <typename R, int SIGN, int LGL>
@@ -1281,10 +1340,11 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 11 + 1];
+  cudaError_t es[8 * 12 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
+  es[n++] = allow_smem(k_zk2<R, LG>, optin);             \
   es[n++] = allow_smem(k_spass<R, 1, LG>, optin);        \
   es[n++] = allow_smem(k_spass<R, -1, LG>, optin);       \
   if (sizeof(R) == 4) {                                  \
@@ -1396,11 +1456,20 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
+    const int split = pm && pm->z_split && c.threads / zcols<R>() <= kSpassThreads ? 1 : 0;
 #define GT_L(LG)                                                                                   \
   k_zinv_curl<R, LG><<<grid, c.threads / zcols<R>(), c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned,    \
-                                                                  tb.ztl[c.lgTX]);
+                                                                  tb.ztl[c.lgTX], split ? 0 : 1);
     GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
+    if (split && !(rc = (int)cudaGetLastError())) {
+      // w = k^2 a: one field per block, one shared region (a third of the smem)
+      const dim3 grid2 = pruned ? dim3(tb.nztl[c.lgTX], 3) : dim3(c.ntiles, 3, g.ny);
+      const int smem1 = c.smem / 3;
+#define GT_L(LG) k_zk2<R, LG><<<grid2, c.threads / zcols<R>(), smem1, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    }
     GT_HOOK(kKZinvCurl, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }

@@ -192,7 +192,8 @@ int gt_set_pipelining(gt_handle* h, int32_t enable);
  * with the lines transformed one by one; 0 = three groups per row pair), "y_pairs" (0/1: FP32 y passes with
  * two adjacent columns per thread, or one), "fuse_stage" (0/1: the first nonlinear
  * term's z forward pass and the second term's z inverse pass as one kernel that
- * keeps the stage value c on chip, or two passes with c in HBM). */
+ * keeps the stage value c on chip, or two passes with c in HBM), "z_split" (0/1:
+ * the z inverse pass's w = k^2 a in its own one-region kernel). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 
 /* Allocation-free kinetic energy, for callers that cannot allocate device

@@ -159,3 +159,24 @@ def test_fused_stage_boundary_equals_separate_passes(lib, n, precision, tol, tru
         a.step(3, 5)
         b.step(3, 5)
         assert relerr(a.get_state(), b.get_state()) < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,precision,tol", [(32, "fp64", 1e-14), (64, "mixed", 1e-6), ((16, 64, 32), "mixed", 1e-6),
+                                             ((64, 16, 1024), "fp64", 1e-14), ((8, 8, 16), "mixed", 1e-6)])
+@pytest.mark.parametrize("truncate", [1, 0])
+def test_split_z_inverse_equals_combined(lib, n, precision, tol, truncate):
+    """The z inverse pass with w = k^2 a in its own one-region kernel gives the
+    result of the combined three-region kernel."""
+    import gturbo3d_gb300 as g
+    gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate)
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(n, seed=15)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        b.set_state(b0)
+        a.set_tuning("z_split", 1)
+        b.set_tuning("z_split", 0)
+        a.step(3, 5)
+        b.step(3, 5)
+        assert relerr(a.get_state(), b.get_state()) < tol
