@@ -38,7 +38,8 @@ def test_rann_matches_oracle(lib):
 @pytest.mark.parametrize("kind,k1f,k2f,nf_expected", [("3d3c", 1.999, 3.0, 48), ("3d3c", 2.0, 3.0, 45),
                                                        ("2d2c", 1.999, 3.0, 10)])
 def test_forced_mode_counts(lib, kind, k1f, k2f, nf_expected):
-    """Lattice-point counts in the half space (SURVEY known answers)."""
+    """Lattice-point counts of the forced shells in the half space (known answers
+    from counting integer wavevectors with k1f < |k| <= k2f)."""
     import gturbo3d_gb300 as g
     from oracle.gturbo_oracle import Params, defk, iniforcing
     p = g.make_params(64, forcing=kind, k1f=k1f, k2f=k2f, famp=0.5)
