@@ -147,3 +147,44 @@ def test_oracle_reproduces_golden_trace(name):
     b, s = o.run(b0, int(g["seed0"]), 2)
     assert s == int(g["seed_2"])
     assert relerr(b, list(g["b_2"])) < 1e-14
+
+
+def test_spectrum_sums_to_energy():
+    """For a solenoidal, truncated state |k x b|^2 = k^2 |b|^2, so the shell
+    spectrum E(k) (diagnostics.f90:22-53) sums to glob's energy when no mode
+    falls beyond the last bin (|k| <= N/3 < N/2 - 1)."""
+    from gturbo3d_gb300.synth import initial_potential
+    from oracle.gturbo_oracle import Params, defk, energy, spectrum
+    p = Params(nx=32, ny=32, nz=32)
+    wk = defk(p)
+    b = initial_potential(32, 32, 32, 5)
+    ek, _ = spectrum(b, p, wk)
+    e = energy(b, p, wk)
+    assert abs(ek.sum() - e) <= 1e-13 * e
+
+
+def test_beltrami_helicity_is_k_times_energy():
+    """An ABC flow with |k| = 1 has w = curl u = u, so H = sum fac Re(u . w*)
+    equals sum fac |u|^2 = E."""
+    from oracle.gturbo_oracle import energy, helicity
+    b, p, wk = _abc_potential(16)
+    e = energy(b, p, wk)
+    assert abs(helicity(b, p, wk) - e) <= 1e-13 * e
+
+
+def test_total_nonlinear_transfer_vanishes():
+    """u . (u x w) = 0 pointwise and the truncated state has no modes outside
+    the kept set, so the energy transfer summed over all shells (the flux at
+    the first shell, diagnostics.f90:77-100) vanishes, with or without the
+    Coriolis term (i Omega kz b contributes Re(i |b|^2) = 0)."""
+    from gturbo3d_gb300.synth import initial_potential
+    from oracle.gturbo_oracle import Params, defk, fluxes, nlt
+    for omega in (0.0, 5.0):
+        p = Params(nx=32, ny=32, nz=32, omega=omega)
+        wk = defk(p)
+        b = initial_potential(32, 32, 32, 6)
+        n1 = nlt(b, b, p, wk)
+        fl = fluxes(b, n1, p, wk)
+        scale = np.abs(np.diff(fl)).sum()          # the shell transfers themselves
+        assert scale > 0
+        assert abs(fl[0]) <= 1e-12 * scale
