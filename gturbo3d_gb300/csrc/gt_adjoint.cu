@@ -1,6 +1,6 @@
 // Building blocks of the tangent-linear and adjoint RK2 step: pointwise
 // operators on groups of three spectral fields and on three real physical
-// fields.  The step algebra itself is composed on the host (gt_capi.cu).
+// fields.  The step algebra itself is composed on the host (gt_tl_adj.cu).
 //
 // Inner products.  Spectral fields represent real fields; the adjoint is
 // taken with respect to <x, y> = sum over stored modes of w_k Re(conj(x_k) y_k),

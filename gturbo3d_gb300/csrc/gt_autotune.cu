@@ -1,0 +1,189 @@
+// C-ABI autotuner of the launch-shape knobs.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gt_fft.cuh"
+#include "gt_handle.h"
+#include "gt_internal.h"
+
+using namespace gt;
+using namespace gtc;
+
+// ===========================================================================
+// Autotuner: coordinate descent over the launch-shape knobs of the pipelined
+// passes, timing whole RK2 steps with CUDA events on a copy of the state;
+// the choice is cached per (grid, precision, pruning, GPU) in a JSON-lines
+// file.
+// ===========================================================================
+
+Tuning gtc::get_tuning(const gt_handle* h) {
+  return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
+                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs, h->pm.fuse_stage, h->pm.z_split};
+}
+
+void gtc::put_tuning(gt_handle* h, const Tuning& t) {
+  h->pm.pipe_y = t.pipe_y;
+  h->pm.pipe_z = t.pipe_z;
+  h->pm.pipe_x = t.pipe_x;
+  h->pm.x_pairs = t.x_pairs;
+  h->pm.x_stages = t.x_stages;
+  h->pm.y_tx = t.y_tx;
+  h->pm.z_tx = t.z_tx;
+  h->pm.x_fused = t.x_fused;
+  h->pm.y_pairs = t.y_pairs;
+  h->pm.fuse_stage = t.fuse_stage;
+  h->pm.z_split = t.z_split;
+}
+
+std::string gtc::tuning_key(const gt_handle* h) {
+  cudaDeviceProp prop;
+  std::string name = "gpu";
+  if (cudaGetDeviceProperties(&prop, h->p.device) == cudaSuccess) name = prop.name;
+  for (char& c : name)
+    if (c == '"' || c == ' ') c = '_';
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%dx%dx%d/%s/%s/%s", h->g.nx, h->g.ny, h->g.nz,
+                h->mixed ? "mixed" : "fp64", use_pruning(h) ? "pruned" : "full", name.c_str());
+  return buf;
+}
+
+namespace {
+
+bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[1024];
+  bool found = false;
+  const std::string pat = "\"key\": \"" + key + "\"";
+  while (std::fgets(line, sizeof line, f)) {
+    if (!std::strstr(line, pat.c_str())) continue;
+    Tuning u{};
+    auto get = [&](const char* name, int& v) {
+      const char* q = std::strstr(line, name);
+      return q && std::sscanf(q + std::strlen(name), "%d", &v) == 1;
+    };
+    if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
+        get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
+        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
+        get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage) &&
+        get("\"z_split\": ", u.z_split)) {
+      t = u;
+      found = true;   // the last matching line wins
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+void cache_store(const char* path, const std::string& key, const Tuning& t, double ms) {
+  if (!path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f,
+               "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
+               "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
+               "\"y_pairs\": %d, \"fuse_stage\": %d, \"z_split\": %d, \"ms_per_step\": %.6f}\n",
+               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused,
+               t.y_pairs, t.fuse_stage, t.z_split, ms);
+  std::fclose(f);
+}
+
+// Mean ms of `steps` RK2 steps (no forcing: the kernels are the same).
+int time_steps(gt_handle* h, int steps, double* ms) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::vector<ForceEntry> none;
+  std::vector<size_t> offs(steps + 1, 0);
+  int rc = run_steps(h, 1, none, offs);   // warm-up (and lazy attribute set-up)
+  if (!rc) {
+    cudaEventRecord(e0, h->stream);
+    rc = run_steps(h, steps, none, offs);
+    cudaEventRecord(e1, h->stream);
+  }
+  if (!rc) {
+    CK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t / steps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+}  // namespace
+
+int gtc::autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
+  const std::string key = tuning_key(h);
+  Tuning t{};
+  if (cache_lookup(cache_path, key, t)) {
+    put_tuning(h, t);
+    if (best_ms_out) *best_ms_out = -1.0;
+    return GT_OK;
+  }
+  // the timing steps overwrite the state: keep a copy
+  const size_t bytes = h->g.field_elems() * h->csize;
+  void* save = nullptr;
+  CK(cudaMalloc(&save, 3 * bytes));
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpyAsync((char*)save + c * bytes, h->b[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
+  const bool was_in_k = h->state_in_k;
+  auto restore = [&]() {
+    for (int c = 0; c < 3; ++c)
+      cudaMemcpyAsync(h->b[c], (char*)save + c * bytes, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    h->state_in_k = was_in_k;
+  };
+  Tuning best = get_tuning(h);
+  double best_ms = 0;
+  int rc = time_steps(h, 3, &best_ms);
+  if (rc) { restore(); cudaFree(save); return rc; }
+  // enough steps per timing for about 30 ms of work (small grids are noisy)
+  const int nt = (int)std::min(200.0, std::max(3.0, std::ceil(30.0 / std::max(best_ms, 1e-3))));
+  if (nt > 3 && (rc = time_steps(h, nt, &best_ms))) { restore(); cudaFree(save); return rc; }
+  struct Knob { int Tuning::*field; std::vector<int> values; };
+  const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
+                                   {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
+                                   {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
+                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1, 2}},
+                                   {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}},
+                                   {&Tuning::z_split, {0, 1}}};
+  for (const Knob& k : knobs) {
+    for (int v : k.values) {
+      if (best.*(k.field) == v) continue;
+      Tuning cand = best;
+      cand.*(k.field) = v;
+      put_tuning(h, cand);
+      double ms = 0;
+      // a candidate must beat the incumbent by 2 % (timing noise)
+      if (time_steps(h, nt, &ms) == GT_OK && ms < 0.98 * best_ms) {
+        best_ms = ms;
+        best = cand;
+      }
+      cudaGetLastError();   // a shape the device rejects is simply skipped
+    }
+  }
+  put_tuning(h, best);
+  restore();
+  cudaFree(save);
+  cache_store(cache_path, key, best, best_ms);
+  if (best_ms_out) *best_ms_out = best_ms;
+  return GT_OK;
+}
+
+extern "C" {
+
+int gt_autotune(gt_handle* h, const char* cache_path, double* best_ms) {
+  if (!h) return GT_EINVAL;
+  int rc = set_dev(h);
+  if (rc) return rc;
+  return autotune_handle(h, cache_path, best_ms);
+}
+
+}  // extern "C"

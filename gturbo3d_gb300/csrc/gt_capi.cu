@@ -10,86 +10,26 @@
 #include <vector>
 
 #include "gt_fft.cuh"
+#include "gt_handle.h"
 #include "gt_internal.h"
 
 using namespace gt;
+using namespace gtc;
 
 namespace {
 
 thread_local std::string g_last_error;
 
-int cuda_fail(cudaError_t e, const char* what) {
+}  // namespace
+
+int gtc::cuda_fail(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
   return GT_ECUDA;
 }
 
-#define CK(call)                                   \
-  do {                                             \
-    cudaError_t e_ = (call);                       \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-  } while (0)
-
-#define CKI(rcexpr)                                                  \
-  do {                                                               \
-    int r_ = (rcexpr);                                               \
-    if (r_ != 0) return cuda_fail((cudaError_t)r_, #rcexpr);         \
-  } while (0)
-
-struct Pending {
-  int kind;
-  cudaEvent_t e0, e1;
-};
-
-}  // namespace
-
 void gt::set_last_error(const std::string& msg) { g_last_error = msg; }
 
-struct gt_handle {
-  gt_params p{};
-  HostTables ht;
-  Geom g{};
-  int mixed = 0;
-  int csize = 16;
-  cudaStream_t stream = nullptr;
-  void* fields_mem = nullptr;
-  void* b[3]{};
-  void* c[3]{};
-  void* w[6]{};
-  void* stage = nullptr;       // one FP64 spectral field [nz][ny][nhp] double2
-  void* tab_mem = nullptr;
-  DevTables<double> t64{};
-  DevTables<float> t32{};
-  // forcing entries: double-buffered pinned staging and device buffers
-  ForceEntry* d_force[2]{};
-  ForceEntry* h_force[2]{};
-  size_t force_cap[2]{};
-  cudaEvent_t force_copied[2]{};
-  int force_slot = 0;
-  double* d_partials = nullptr;
-  int npartials = 0;
-  double* d_result = nullptr;
-  double* h_result = nullptr;
-  int nresult = 0;
-  int64_t launches = 0;
-  // truncation-aware pruning: allowed by the caller, the state is zero outside
-  // the kept set K, and every forced mode lies in K
-  bool prune_enabled = true;
-  bool state_in_k = false;
-  bool forcing_in_k = false;
-  unsigned long long* d_count = nullptr;
-  // TMA-pipelined y passes (maps of the six work fields) and the device error
-  // flag their bounded waits raise
-  PipeMaps pm{};
-  bool use_pipe = true;
-  int* d_err = nullptr;
-  bool prof = false;
-  std::vector<Pending> pending;
-  std::vector<cudaEvent_t> pool;
-  int64_t kind_launches[kNumKinds]{};
-  double kind_ms[kNumKinds]{};
-};
-
-namespace {
+namespace gtc {
 
 void hook_fn(void* ctx, int kind, bool begin) {
   gt_handle* h = static_cast<gt_handle*>(ctx);
@@ -298,7 +238,7 @@ PipeMaps effective_tuning(const gt_handle* h) {
 }
 
 int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
-        int pruned = 0) {
+        int pruned) {
   const PipeMaps pm = effective_tuning(h);
   if (h->mixed)
     return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, &pm, h->d_err, h->stream,
@@ -478,7 +418,7 @@ int set_dev(gt_handle* h) {
   return GT_OK;
 }
 
-}  // namespace
+}  // namespace gtc
 
 extern "C" {
 
@@ -874,787 +814,5 @@ int gt_profile_read(gt_handle* h, int32_t cap, char* names, int64_t* launches, d
 }
 
 const char* gt_last_error(void) { return g_last_error.c_str(); }
-
-}  // extern "C"
-
-// ===========================================================================
-// Autotuner: coordinate descent over the launch-shape knobs of the pipelined
-// passes, timing whole RK2 steps with CUDA events on a copy of the state;
-// the choice is cached per (grid, precision, pruning, GPU) in a JSON-lines
-// file.
-// ===========================================================================
-namespace {
-
-struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split;
-};
-
-Tuning get_tuning(const gt_handle* h) {
-  return Tuning{h->pm.pipe_y, h->pm.pipe_z, h->pm.pipe_x, h->pm.x_pairs, h->pm.x_stages, h->pm.y_tx,
-                h->pm.z_tx, h->pm.x_fused, h->pm.y_pairs, h->pm.fuse_stage, h->pm.z_split};
-}
-
-void put_tuning(gt_handle* h, const Tuning& t) {
-  h->pm.pipe_y = t.pipe_y;
-  h->pm.pipe_z = t.pipe_z;
-  h->pm.pipe_x = t.pipe_x;
-  h->pm.x_pairs = t.x_pairs;
-  h->pm.x_stages = t.x_stages;
-  h->pm.y_tx = t.y_tx;
-  h->pm.z_tx = t.z_tx;
-  h->pm.x_fused = t.x_fused;
-  h->pm.y_pairs = t.y_pairs;
-  h->pm.fuse_stage = t.fuse_stage;
-  h->pm.z_split = t.z_split;
-}
-
-std::string tuning_key(const gt_handle* h) {
-  cudaDeviceProp prop;
-  std::string name = "gpu";
-  if (cudaGetDeviceProperties(&prop, h->p.device) == cudaSuccess) name = prop.name;
-  for (char& c : name)
-    if (c == '"' || c == ' ') c = '_';
-  char buf[256];
-  std::snprintf(buf, sizeof buf, "%dx%dx%d/%s/%s/%s", h->g.nx, h->g.ny, h->g.nz,
-                h->mixed ? "mixed" : "fp64", use_pruning(h) ? "pruned" : "full", name.c_str());
-  return buf;
-}
-
-bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
-  if (!path) return false;
-  FILE* f = std::fopen(path, "r");
-  if (!f) return false;
-  char line[1024];
-  bool found = false;
-  const std::string pat = "\"key\": \"" + key + "\"";
-  while (std::fgets(line, sizeof line, f)) {
-    if (!std::strstr(line, pat.c_str())) continue;
-    Tuning u{};
-    auto get = [&](const char* name, int& v) {
-      const char* q = std::strstr(line, name);
-      return q && std::sscanf(q + std::strlen(name), "%d", &v) == 1;
-    };
-    if (get("\"pipe_y\": ", u.pipe_y) && get("\"pipe_z\": ", u.pipe_z) && get("\"pipe_x\": ", u.pipe_x) &&
-        get("\"x_pairs\": ", u.x_pairs) && get("\"x_stages\": ", u.x_stages) &&
-        get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
-        get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage) &&
-        get("\"z_split\": ", u.z_split)) {
-      t = u;
-      found = true;   // the last matching line wins
-    }
-  }
-  std::fclose(f);
-  return found;
-}
-
-void cache_store(const char* path, const std::string& key, const Tuning& t, double ms) {
-  if (!path) return;
-  FILE* f = std::fopen(path, "a");
-  if (!f) return;
-  std::fprintf(f,
-               "{\"key\": \"%s\", \"pipe_y\": %d, \"pipe_z\": %d, \"pipe_x\": %d, \"x_pairs\": %d, "
-               "\"x_stages\": %d, \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
-               "\"y_pairs\": %d, \"fuse_stage\": %d, \"z_split\": %d, \"ms_per_step\": %.6f}\n",
-               key.c_str(), t.pipe_y, t.pipe_z, t.pipe_x, t.x_pairs, t.x_stages, t.y_tx, t.z_tx, t.x_fused,
-               t.y_pairs, t.fuse_stage, t.z_split, ms);
-  std::fclose(f);
-}
-
-// Mean ms of `steps` RK2 steps (no forcing: the kernels are the same).
-int time_steps(gt_handle* h, int steps, double* ms) {
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
-  std::vector<ForceEntry> none;
-  std::vector<size_t> offs(steps + 1, 0);
-  int rc = run_steps(h, 1, none, offs);   // warm-up (and lazy attribute set-up)
-  if (!rc) {
-    cudaEventRecord(e0, h->stream);
-    rc = run_steps(h, steps, none, offs);
-    cudaEventRecord(e1, h->stream);
-  }
-  if (!rc) {
-    CK(cudaEventSynchronize(e1));
-    float t = 0.f;
-    cudaEventElapsedTime(&t, e0, e1);
-    *ms = t / steps;
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  return rc;
-}
-
-int autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_out) {
-  const std::string key = tuning_key(h);
-  Tuning t{};
-  if (cache_lookup(cache_path, key, t)) {
-    put_tuning(h, t);
-    if (best_ms_out) *best_ms_out = -1.0;
-    return GT_OK;
-  }
-  // the timing steps overwrite the state: keep a copy
-  const size_t bytes = h->g.field_elems() * h->csize;
-  void* save = nullptr;
-  CK(cudaMalloc(&save, 3 * bytes));
-  for (int c = 0; c < 3; ++c)
-    CK(cudaMemcpyAsync((char*)save + c * bytes, h->b[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
-  const bool was_in_k = h->state_in_k;
-  auto restore = [&]() {
-    for (int c = 0; c < 3; ++c)
-      cudaMemcpyAsync(h->b[c], (char*)save + c * bytes, bytes, cudaMemcpyDeviceToDevice, h->stream);
-    cudaStreamSynchronize(h->stream);
-    h->state_in_k = was_in_k;
-  };
-  Tuning best = get_tuning(h);
-  double best_ms = 0;
-  int rc = time_steps(h, 3, &best_ms);
-  if (rc) { restore(); cudaFree(save); return rc; }
-  // enough steps per timing for about 30 ms of work (small grids are noisy)
-  const int nt = (int)std::min(200.0, std::max(3.0, std::ceil(30.0 / std::max(best_ms, 1e-3))));
-  if (nt > 3 && (rc = time_steps(h, nt, &best_ms))) { restore(); cudaFree(save); return rc; }
-  struct Knob { int Tuning::*field; std::vector<int> values; };
-  const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},  {&Tuning::z_tx, {0, 4, 8}},
-                                   {&Tuning::pipe_y, {0, 1}},    {&Tuning::pipe_z, {0, 1}},
-                                   {&Tuning::pipe_x, {0, 1}},    {&Tuning::x_pairs, {1, 2}},
-                                   {&Tuning::x_stages, {2, 3}},  {&Tuning::x_fused, {0, 1, 2}},
-                                   {&Tuning::y_pairs, {0, 1}},   {&Tuning::fuse_stage, {0, 1}},
-                                   {&Tuning::z_split, {0, 1}}};
-  for (const Knob& k : knobs) {
-    for (int v : k.values) {
-      if (best.*(k.field) == v) continue;
-      Tuning cand = best;
-      cand.*(k.field) = v;
-      put_tuning(h, cand);
-      double ms = 0;
-      // a candidate must beat the incumbent by 2 % (timing noise)
-      if (time_steps(h, nt, &ms) == GT_OK && ms < 0.98 * best_ms) {
-        best_ms = ms;
-        best = cand;
-      }
-      cudaGetLastError();   // a shape the device rejects is simply skipped
-    }
-  }
-  put_tuning(h, best);
-  restore();
-  cudaFree(save);
-  cache_store(cache_path, key, best, best_ms);
-  if (best_ms_out) *best_ms_out = best_ms;
-  return GT_OK;
-}
-
-}  // namespace
-
-// ===========================================================================
-// Tangent-linear and adjoint RK2 step (the differentiation extension).
-// With a the stage input, bc the Coriolis source and Q(a) = P invcurl
-// fft_dir(u(a) x w(a)):  nlt(a; bc) = Q(a) + P invcurl(i omega kz bc).
-//   TL:  dN = P invcurl[ fft_dir(du x w + u x dw) + i omega kz dbc ]
-//   adjoint (inner products of gt_adjoint.cu): with mu = invcurl P lam and
-//   g = fft_inv(mu):  lam_a = curl fft_dir(w x g) + k^2 fft_dir(g x u),
-//   lam_bc = -i omega kz mu.
-// The RK2 step and its zeroing of the k = 0 mode (rkstep.f90:140-144,
-// 196-200) are differentiated on top.
-// ===========================================================================
-namespace {
-
-enum SpecOp { kOpCurl = 0, kOpK2 = 1, kOpInvcurl = 2, kOpTrunc = 3, kOpCoriolis = 4, kOpEmk = 5,
-              kOpCopy = 6, kOpShell = 7, kOpZero0 = 8 };
-
-struct F3 {
-  void* p[3];
-};
-
-template <typename R>
-struct AdjWork {
-  gt_handle* h;
-  const DevTables<R>& tb;
-  std::vector<void*> blocks;
-  size_t sbytes, rbytes;
-  AdjWork(gt_handle* hh, const DevTables<R>& t) : h(hh), tb(t) {
-    sbytes = h->g.field_elems() * sizeof(Cplx<R>);
-    rbytes = (size_t)h->g.nx * h->g.ny * h->g.nz * sizeof(R);
-  }
-  ~AdjWork() {
-    for (void* p : blocks) cudaFree(p);
-  }
-  int alloc(F3& f, bool real) {
-    void* p = nullptr;
-    const size_t b = real ? rbytes : sbytes;
-    cudaError_t e = cudaMalloc(&p, 3 * b);
-    if (e != cudaSuccess) return cuda_fail(e, "adjoint workspace");
-    blocks.push_back(p);
-    for (int c = 0; c < 3; ++c) f.p[c] = (char*)p + c * b;
-    return GT_OK;
-  }
-  int op(const F3& out, const F3& a, const F3* b, int o, double sgn = 1, double kmin2 = 0, double beta = 0) {
-    CKI(launch_spec_op<R>(h->g, tb, out.p, a.p, b ? b->p : nullptr, o, sgn, kmin2, beta, h->stream));
-    return GT_OK;
-  }
-  // real = C2R(spec); spec is destroyed
-  int inv(const F3& real, const F3& spec) {
-    for (int c = 0; c < 3; ++c)
-      CKI(launch_fft_inv<R>(h->g, tb, spec.p[c], real.p[c], h->w, h->stream, hook_fn, h));
-    return GT_OK;
-  }
-  int dir(const F3& spec, const F3& real) {
-    for (int c = 0; c < 3; ++c)
-      CKI(launch_fft_dir<R>(h->g, tb, real.p[c], spec.p[c], h->w, h->stream, hook_fn, h));
-    return GT_OK;
-  }
-  int cross(const F3& out, const F3& a, const F3& b, const F3* c = nullptr, const F3* d = nullptr) {
-    CKI(launch_phys_cross<R>(h->g, out.p, a.p, b.p, c ? c->p : nullptr, d ? d->p : nullptr, 1.0, 1.0,
-                             h->stream));
-    return GT_OK;
-  }
-};
-
-// u = C2R(curl a), w = C2R(k^2 a) (tmp: one spectral group of scratch)
-template <typename R>
-int phys_uw(AdjWork<R>& W, const F3& a, const F3& u, const F3& w, const F3& tmp) {
-  int rc;
-  if ((rc = W.op(tmp, a, nullptr, kOpCurl))) return rc;
-  if ((rc = W.inv(u, tmp))) return rc;
-  if ((rc = W.op(tmp, a, nullptr, kOpK2))) return rc;
-  return W.inv(w, tmp);
-}
-
-// dN = TL of nlt at (a; bc) in direction (da; dbc)
-template <typename R>
-int tl_nlt(AdjWork<R>& W, const F3& a, const F3& da, const F3& dbc, const F3& dN, const F3 s[2],
-           const F3 r[5]) {
-  int rc;
-  if ((rc = phys_uw(W, a, r[0], r[1], s[0]))) return rc;      // u, w
-  if ((rc = phys_uw(W, da, r[2], r[3], s[0]))) return rc;     // du, dw
-  if ((rc = W.cross(r[4], r[2], r[1], &r[0], &r[3]))) return rc;   // du x w + u x dw
-  if ((rc = W.dir(s[0], r[4]))) return rc;
-  if ((rc = W.op(s[1], dbc, &s[0], kOpCoriolis, +1.0, 0, 1.0))) return rc;   // + i omega kz dbc
-  if ((rc = W.op(s[0], s[1], nullptr, kOpInvcurl))) return rc;
-  return W.op(dN, s[0], nullptr, kOpTrunc);
-}
-
-// (lam_a, lam_bc) += adjoint of tl_nlt at (a; bc) applied to lam
-template <typename R>
-int adj_nlt(AdjWork<R>& W, const F3& a, const F3& lam, const F3& lam_a, const F3& lam_bc, const F3 s[3],
-            const F3 r[5]) {
-  int rc;
-  if ((rc = W.op(s[0], lam, nullptr, kOpTrunc))) return rc;
-  if ((rc = W.op(s[1], s[0], nullptr, kOpInvcurl))) return rc;              // mu
-  if ((rc = W.op(lam_bc, s[1], &lam_bc, kOpCoriolis, -1.0, 0, 1.0))) return rc;   // lam_bc += -i omega kz mu
-  if ((rc = W.inv(r[4], s[1]))) return rc;                                  // g = C2R(mu)
-  if ((rc = phys_uw(W, a, r[0], r[1], s[0]))) return rc;                    // u, w
-  if ((rc = W.cross(r[2], r[1], r[4]))) return rc;                          // w x g
-  if ((rc = W.cross(r[3], r[4], r[0]))) return rc;                          // g x u
-  if ((rc = W.dir(s[0], r[2]))) return rc;
-  if ((rc = W.op(s[2], s[0], &lam_a, kOpCurl, 1, 0, 1.0))) return rc;     // lam_a + curl(.)
-  if ((rc = W.dir(s[0], r[3]))) return rc;
-  return W.op(lam_a, s[0], &s[2], kOpK2, 1, 0, 1.0);                        // + k^2(.)
-}
-
-template <typename R>
-struct StepCtx {
-  AdjWork<R> W;
-  F3 s[3], r[5], n1, c, t1, t2, t3;
-  StepCtx(gt_handle* h, const DevTables<R>& tb) : W(h, tb) {}
-  int init() {
-    int rc = 0;
-    for (int i = 0; i < 3 && !rc; ++i) rc = W.alloc(s[i], false);
-    for (int i = 0; i < 5 && !rc; ++i) rc = W.alloc(r[i], true);
-    if (!rc) rc = W.alloc(n1, false);
-    if (!rc) rc = W.alloc(c, false);
-    if (!rc) rc = W.alloc(t1, false);
-    if (!rc) rc = W.alloc(t2, false);
-    if (!rc) rc = W.alloc(t3, false);
-    return rc;
-  }
-  // c = E(b + dt2 N1(b)), c(0) = 0, for the state b in the handle
-  int stage(const F3& b) {
-    gt_handle* h = W.h;
-    CKI(nlt(h, b.p, b.p, n1.p, kNltOnly, 0));
-    int rc;
-    if ((rc = W.op(t3, b, &n1, kOpCopy, 1, 0, (double)W.tb.dt2))) return rc;
-    if ((rc = W.op(c, t3, nullptr, kOpEmk))) return rc;
-    return W.op(c, c, nullptr, kOpZero0);
-  }
-  // db' = TL of the RK2 step at b applied to db
-  int tl(const F3& b, const F3& db, const F3& out) {
-    int rc;
-    if ((rc = stage(b))) return rc;
-    if ((rc = tl_nlt(W, b, db, db, t1, s, r))) return rc;                    // dN1
-    if ((rc = W.op(t2, db, &t1, kOpCopy, 1, 0, (double)W.tb.dt2))) return rc;  // db + dt2 dN1
-    if ((rc = W.op(t3, t2, nullptr, kOpEmk))) return rc;
-    if ((rc = W.op(t3, t3, nullptr, kOpZero0))) return rc;                   // dc
-    if ((rc = tl_nlt(W, c, t3, db, t1, s, r))) return rc;                    // dN2
-    if ((rc = W.op(t2, db, nullptr, kOpEmk))) return rc;                     // E db
-    if ((rc = W.op(t2, t2, &t1, kOpCopy, 1, 0, (double)W.tb.dt))) return rc;  // + dt dN2
-    if ((rc = W.op(out, t2, nullptr, kOpEmk))) return rc;
-    return W.op(out, out, nullptr, kOpZero0);
-  }
-  // lam = adjoint of the RK2 step at b applied to lam' (in: lp, out: out)
-  int adj(const F3& b, const F3& lp, const F3& out) {
-    int rc;
-    if ((rc = stage(b))) return rc;
-    if ((rc = W.op(t1, lp, nullptr, kOpZero0))) return rc;                   // Z lam'
-    if ((rc = W.op(t2, t1, nullptr, kOpEmk))) return rc;                     // E Z lam'
-    if ((rc = W.op(out, t2, nullptr, kOpEmk))) return rc;                    // lam_b = E E Z lam'
-    if ((rc = W.op(t1, t2, nullptr, kOpCopy, 1, 0, 0))) return rc;
-    if ((rc = W.op(t2, t2, &t2, kOpCopy, 1, 0, (double)W.tb.dt - 1.0))) return rc;   // lam_N2 = dt E Z lam'
-    // lam_c (in t3, from zero) and lam_b += lam_bc2
-    if ((rc = W.op(t3, t3, nullptr, kOpCopy, 1, 0, 0))) return rc;
-    CK(cudaMemsetAsync(t3.p[0], 0, W.sbytes, W.h->stream));
-    CK(cudaMemsetAsync(t3.p[1], 0, W.sbytes, W.h->stream));
-    CK(cudaMemsetAsync(t3.p[2], 0, W.sbytes, W.h->stream));
-    if ((rc = adj_nlt(W, c, t2, t3, out, s, r))) return rc;
-    if ((rc = W.op(t3, t3, nullptr, kOpZero0))) return rc;                   // Z lam_c
-    if ((rc = W.op(t1, t3, nullptr, kOpEmk))) return rc;                     // E lam_c
-    if ((rc = W.op(out, t1, &out, kOpCopy, 1, 0, 1.0))) return rc;           // lam_b += E lam_c
-    if ((rc = W.op(t2, t1, &t1, kOpCopy, 1, 0, (double)W.tb.dt2 - 1.0))) return rc;  // lam_N1 = dt2 E lam_c
-    return adj_nlt(W, b, t2, out, out, s, r);                                // lam_b += lam_a1 + lam_bc1
-  }
-};
-
-template <typename R>
-const DevTables<R>& tables(gt_handle* h);
-template <>
-const DevTables<float>& tables<float>(gt_handle* h) { return h->t32; }
-template <>
-const DevTables<double>& tables<double>(gt_handle* h) { return h->t64; }
-
-template <typename R>
-int tl_or_adj(gt_handle* h, const double* in[3], double* out[3], bool adjoint) {
-  StepCtx<R> S(h, tables<R>(h));
-  int rc = S.init();
-  if (rc) return rc;
-  F3 x, y, b;
-  if ((rc = S.W.alloc(x, false)) || (rc = S.W.alloc(y, false))) return rc;
-  for (int c = 0; c < 3; ++c) {
-    if ((rc = upload_spec(h, in[c], x.p[c]))) return rc;
-    CK(cudaStreamSynchronize(h->stream));
-    b.p[c] = h->b[c];
-  }
-  rc = adjoint ? S.adj(b, x, y) : S.tl(b, x, y);
-  if (rc) return rc;
-  for (int c = 0; c < 3; ++c) {
-    if ((rc = download_spec(h, y.p[c], out[c]))) return rc;
-    CK(cudaStreamSynchronize(h->stream));
-  }
-  return check_device_flag(h);
-}
-
-// J = sum over stored modes with |k| >= kmin of fac |(curl b)_k|^2
-template <typename R>
-int objective(gt_handle* h, StepCtx<R>& S, const F3& b, double kmin, double* J) {
-  int rc;
-  if ((rc = S.W.op(S.t1, b, nullptr, kOpCurl))) return rc;
-  if ((rc = S.W.op(S.t1, S.t1, nullptr, kOpShell, 1, kmin * kmin))) return rc;
-  const Geom& g = h->g;
-  double acc = 0.0;
-  std::vector<double> host((size_t)g.nz * g.ny * g.nh * 2);
-  for (int c = 0; c < 3; ++c) {
-    if ((rc = download_spec(h, S.t1.p[c], host.data()))) return rc;
-    CK(cudaStreamSynchronize(h->stream));
-    for (size_t row = 0; row < (size_t)g.nz * g.ny; ++row)
-      for (int X = 0; X < g.nh; ++X) {
-        const double fac = (X == 0 || X == g.nh - 1) ? 0.5 : 1.0;
-        const double re = host[(row * g.nh + X) * 2], im = host[(row * g.nh + X) * 2 + 1];
-        acc += fac * (re * re + im * im);
-      }
-  }
-  *J = acc;
-  return GT_OK;
-}
-
-template <typename R>
-int gradient(gt_handle* h, int nsteps, int32_t seed, int K, double kmin, double* J, double* gout[3]) {
-  StepCtx<R> S(h, tables<R>(h));
-  int rc = S.init();
-  if (rc) return rc;
-  const size_t fb = S.W.sbytes;
-  const int ncp = (nsteps + K - 1) / K;
-  // checkpoints (state at steps 0, K, 2K, ...) and one segment of states
-  std::vector<F3> cp(std::max(ncp, 1)), seg(K);
-  for (auto& f : cp) if ((rc = S.W.alloc(f, false))) return rc;
-  for (auto& f : seg) if ((rc = S.W.alloc(f, false))) return rc;
-  F3 b0, lam, lam2, state;
-  if ((rc = S.W.alloc(b0, false)) || (rc = S.W.alloc(lam, false)) || (rc = S.W.alloc(lam2, false))) return rc;
-  for (int c = 0; c < 3; ++c) {
-    state.p[c] = h->b[c];
-    CK(cudaMemcpyAsync(b0.p[c], h->b[c], fb, cudaMemcpyDeviceToDevice, h->stream));
-  }
-  const bool was_in_k = h->state_in_k;
-  // the forcing realisation, drawn once and replayed in every recomputation
-  std::vector<ForceEntry> all;
-  std::vector<size_t> offs(1, 0);
-  const bool forced = h->p.forcing != GT_FORCING_NONE && !h->ht.fix.empty();
-  int32_t sd = seed;
-  for (int k = 0; k < nsteps; ++k) {
-    if (forced) draw_forcing(h->p, h->ht, sd, all);
-    offs.push_back(all.size());
-  }
-  auto step_k = [&](int k) {
-    std::vector<ForceEntry> e(all.begin() + offs[k], all.begin() + offs[k + 1]);
-    std::vector<size_t> o = {0, e.size()};
-    return run_steps(h, 1, e, o);
-  };
-  auto copy3 = [&](const F3& dst, const F3& src) {
-    for (int c = 0; c < 3; ++c)
-      cudaMemcpyAsync(dst.p[c], src.p[c], fb, cudaMemcpyDeviceToDevice, h->stream);
-  };
-  for (int k = 0; k < nsteps; ++k) {
-    if (k % K == 0) copy3(cp[k / K], state);
-    if ((rc = step_k(k))) return rc;
-  }
-  if ((rc = objective<R>(h, S, state, kmin, J))) return rc;
-  // lam = dJ/db_n = curl(1_S curl b_n)
-  if ((rc = S.W.op(S.t1, state, nullptr, kOpCurl))) return rc;
-  if ((rc = S.W.op(S.t1, S.t1, nullptr, kOpShell, 1, kmin * kmin))) return rc;
-  if ((rc = S.W.op(lam, S.t1, nullptr, kOpCurl))) return rc;
-  for (int i = ncp - 1; i >= 0; --i) {
-    const int k0 = i * K, k1 = std::min(nsteps, (i + 1) * K);
-    copy3(state, cp[i]);
-    for (int k = k0; k < k1; ++k) {
-      copy3(seg[k - k0], state);
-      if (k + 1 < k1 && (rc = step_k(k))) return rc;
-    }
-    for (int k = k1 - 1; k >= k0; --k) {
-      if ((rc = S.adj(seg[k - k0], lam, lam2))) return rc;
-      copy3(lam, lam2);
-    }
-  }
-  copy3(state, b0);
-  CK(cudaStreamSynchronize(h->stream));
-  h->state_in_k = was_in_k;
-  for (int c = 0; c < 3; ++c) {
-    if ((rc = download_spec(h, lam.p[c], gout[c]))) return rc;
-    CK(cudaStreamSynchronize(h->stream));
-  }
-  return check_device_flag(h);
-}
-
-}  // namespace
-
-extern "C" {
-
-int gt_tl_step(gt_handle* h, const double* dbx, const double* dby, const double* dbz, double* ox,
-               double* oy, double* oz) {
-  if (!h || !dbx || !dby || !dbz || !ox || !oy || !oz) return GT_EINVAL;
-  int rc = set_dev(h);
-  if (rc) return rc;
-  const double* in[3] = {dbx, dby, dbz};
-  double* out[3] = {ox, oy, oz};
-  return h->mixed ? tl_or_adj<float>(h, in, out, false) : tl_or_adj<double>(h, in, out, false);
-}
-
-int gt_adj_step(gt_handle* h, const double* lx, const double* ly, const double* lz, double* ox,
-                double* oy, double* oz) {
-  if (!h || !lx || !ly || !lz || !ox || !oy || !oz) return GT_EINVAL;
-  int rc = set_dev(h);
-  if (rc) return rc;
-  const double* in[3] = {lx, ly, lz};
-  double* out[3] = {ox, oy, oz};
-  return h->mixed ? tl_or_adj<float>(h, in, out, true) : tl_or_adj<double>(h, in, out, true);
-}
-
-int gt_objective(gt_handle* h, double kmin, double* J) {
-  if (!h || !J) return GT_EINVAL;
-  int rc = set_dev(h);
-  if (rc) return rc;
-  F3 b;
-  for (int c = 0; c < 3; ++c) b.p[c] = h->b[c];
-  if (h->mixed) {
-    StepCtx<float> S(h, h->t32);
-    if ((rc = S.init())) return rc;
-    return objective<float>(h, S, b, kmin, J);
-  }
-  StepCtx<double> S(h, h->t64);
-  if ((rc = S.init())) return rc;
-  return objective<double>(h, S, b, kmin, J);
-}
-
-int gt_gradient(gt_handle* h, int32_t nsteps, int32_t seed, int32_t checkpoint_every, double kmin,
-                double* J, double* gx, double* gy, double* gz) {
-  if (!h || nsteps < 1 || checkpoint_every < 1 || !J || !gx || !gy || !gz) return GT_EINVAL;
-  int rc = set_dev(h);
-  if (rc) return rc;
-  double* out[3] = {gx, gy, gz};
-  return h->mixed ? gradient<float>(h, nsteps, seed, checkpoint_every, kmin, J, out)
-                  : gradient<double>(h, nsteps, seed, checkpoint_every, kmin, J, out);
-}
-
-}  // extern "C"
-
-// ===========================================================================
-// Ensemble: independent members of possibly different grids and parameters,
-// advanced together; in graph mode one CUDA graph launch advances every member
-// by one step (each member's kernels on its own stream, forked and joined in
-// the graph), with the forcing drawn on the host per chunk of steps and read
-// on the device by step index.
-// ===========================================================================
-struct gt_ensemble {
-  std::vector<gt_handle*> m;
-  int device = 0;
-  cudaStream_t master = nullptr;
-  cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> join;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  bool dirty = true;
-  int* d_step = nullptr;
-  std::vector<ForceEntry*> d_ent;
-  std::vector<int> n_ent;
-  int chunk_cap = 0;
-  ForceEntry* h_stage = nullptr;
-  size_t h_cap = 0;
-};
-
-namespace {
-
-constexpr int kEnsembleChunk = 64;
-
-void free_ensemble(gt_ensemble* e) {
-  if (!e) return;
-  cudaSetDevice(e->device);
-  if (e->master) cudaStreamSynchronize(e->master);
-  if (e->exec) cudaGraphExecDestroy(e->exec);
-  if (e->graph) cudaGraphDestroy(e->graph);
-  for (auto ev : e->join) cudaEventDestroy(ev);
-  if (e->fork) cudaEventDestroy(e->fork);
-  for (auto p : e->d_ent) if (p) cudaFree(p);
-  if (e->d_step) cudaFree(e->d_step);
-  if (e->h_stage) cudaFreeHost(e->h_stage);
-  for (auto h : e->m) free_handle(h);
-  if (e->master) cudaStreamDestroy(e->master);
-  delete e;
-}
-
-int member_enqueue(gt_ensemble* e, int i) {
-  gt_handle* h = e->m[i];
-  const int pr = use_pruning(h) ? 1 : 0;
-  CKI(rk2_nlts(h, pr));
-  if (e->n_ent[i] > 0) {
-    if (h->mixed)
-      CKI(launch_force_indexed<float>(h->g, h->b, e->d_ent[i], e->n_ent[i], e->d_step + i, h->stream,
-                                      hook_fn, h));
-    else
-      CKI(launch_force_indexed<double>(h->g, h->b, e->d_ent[i], e->n_ent[i], e->d_step + i, h->stream,
-                                       hook_fn, h));
-  }
-  return GT_OK;
-}
-
-// Members by decreasing grid size: the largest members are the critical
-// path, so their work is issued first.
-std::vector<int> launch_order(const gt_ensemble* e) {
-  std::vector<int> order(e->m.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return e->m[a]->g.field_elems() > e->m[b]->g.field_elems();
-  });
-  return order;
-}
-
-// Captures one chunk (kEnsembleChunk steps) of every member: a fork, each
-// member's steps on its own stream, a join.  Members progress independently
-// within the chunk; the only barrier is the join at its end.
-int build_graph(gt_ensemble* e) {
-  if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
-  if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
-  for (auto h : e->m) h->prof = false;
-  CK(cudaStreamBeginCapture(e->master, cudaStreamCaptureModeRelaxed));
-  int rc = GT_OK;
-  cudaEventRecord(e->fork, e->master);
-  for (int i : launch_order(e)) {
-    if (rc) break;
-    cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0);
-    for (int k = 0; k < kEnsembleChunk && !rc; ++k) rc = member_enqueue(e, i);
-    cudaEventRecord(e->join[i], e->m[i]->stream);
-    cudaStreamWaitEvent(e->master, e->join[i], 0);
-  }
-  cudaGraph_t g = nullptr;
-  const cudaError_t ce = cudaStreamEndCapture(e->master, &g);
-  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-  e->graph = g;
-  CK(cudaGraphInstantiate(&e->exec, e->graph, 0));
-  e->dirty = false;
-  return GT_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int gt_autotune(gt_handle* h, const char* cache_path, double* best_ms) {
-  if (!h) return GT_EINVAL;
-  int rc = set_dev(h);
-  if (rc) return rc;
-  return autotune_handle(h, cache_path, best_ms);
-}
-
-int gt_ensemble_create(int32_t n, const gt_params* members, gt_ensemble** out) {
-  if (n <= 0 || !members || !out) return GT_EINVAL;
-  *out = nullptr;
-  gt_ensemble* e = new (std::nothrow) gt_ensemble();
-  if (!e) return GT_ENOMEM;
-  e->device = members[0].device;
-  for (int i = 0; i < n; ++i) {
-    if (members[i].device != e->device) { free_ensemble(e); return GT_EINVAL; }
-    gt_handle* h = nullptr;
-    const int rc = gt_create(&members[i], &h);
-    if (rc) { free_ensemble(e); return rc; }
-    e->m.push_back(h);
-  }
-  cudaSetDevice(e->device);
-  cudaError_t ce = cudaStreamCreateWithFlags(&e->master, cudaStreamNonBlocking);
-  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
-  e->join.assign(n, nullptr);
-  for (int i = 0; i < n && ce == cudaSuccess; ++i) ce = cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming);
-  if (ce == cudaSuccess) ce = cudaMalloc(&e->d_step, n * sizeof(int));
-  if (ce != cudaSuccess) { free_ensemble(e); return cuda_fail(ce, "gt_ensemble_create"); }
-  e->n_ent.assign(n, 0);
-  e->d_ent.assign(n, nullptr);
-  // entries per step are fixed by each member's forced-mode list
-  for (int i = 0; i < n; ++i) {
-    gt_handle* h = e->m[i];
-    if (h->p.forcing == GT_FORCING_NONE || h->ht.fix.empty()) continue;
-    std::vector<ForceEntry> one;
-    int32_t seed = 1;
-    draw_forcing(h->p, h->ht, seed, one);
-    e->n_ent[i] = (int)one.size();
-  }
-  *out = e;
-  return GT_OK;
-}
-
-int gt_ensemble_destroy(gt_ensemble* e) {
-  if (!e) return GT_EINVAL;
-  free_ensemble(e);
-  return GT_OK;
-}
-
-int gt_ensemble_set_state(gt_ensemble* e, int32_t i, const double* bx, const double* by, const double* bz) {
-  if (!e || i < 0 || i >= (int)e->m.size()) return GT_EINVAL;
-  e->dirty = true;
-  return gt_set_state(e->m[i], bx, by, bz);
-}
-
-int gt_ensemble_get_state(gt_ensemble* e, int32_t i, double* bx, double* by, double* bz) {
-  if (!e || i < 0 || i >= (int)e->m.size()) return GT_EINVAL;
-  CK(cudaStreamSynchronize(e->master));
-  return gt_get_state(e->m[i], bx, by, bz);
-}
-
-int gt_ensemble_energy(gt_ensemble* e, double* energy) {
-  if (!e || !energy) return GT_EINVAL;
-  CK(cudaStreamSynchronize(e->master));
-  for (size_t i = 0; i < e->m.size(); ++i) {
-    double ex[3];
-    const int rc = gt_energy(e->m[i], ex);
-    if (rc) return rc;
-    energy[i] = ex[0] + ex[1] + ex[2];
-  }
-  return GT_OK;
-}
-
-int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path) {
-  if (!e) return GT_EINVAL;
-  CK(cudaStreamSynchronize(e->master));
-  // one tuning per distinct (grid, precision) class, applied to every member of the class
-  std::vector<std::pair<std::string, Tuning>> done;
-  for (auto h : e->m) {
-    const std::string key = tuning_key(h);
-    bool have = false;
-    for (auto& d : done)
-      if (d.first == key) { put_tuning(h, d.second); have = true; }
-    if (have) continue;
-    const int rc = gt_autotune(h, cache_path, nullptr);
-    if (rc) return rc;
-    done.emplace_back(key, get_tuning(h));
-  }
-  e->dirty = true;
-  return GT_OK;
-}
-
-int gt_ensemble_step(gt_ensemble* e, int32_t nsteps, int32_t* seeds, int32_t graph) {
-  if (!e || nsteps < 0) return GT_EINVAL;
-  const int n = (int)e->m.size();
-  bool forced = false;
-  for (int i = 0; i < n; ++i) forced = forced || e->n_ent[i] > 0;
-  if (forced && !seeds) return GT_EINVAL;
-  CK(cudaSetDevice(e->device));
-  for (auto h : e->m)
-    CK(cudaStreamSynchronize(h->stream));
-  int done = 0;
-  while (done < nsteps) {
-    const int K = std::min(kEnsembleChunk, nsteps - done);
-    // draw and upload K steps of forcing per member
-    size_t total = 0;
-    for (int i = 0; i < n; ++i) total += (size_t)K * e->n_ent[i];
-    CK(cudaStreamSynchronize(e->master));   // the staging buffer is free
-    if (total > e->h_cap) {
-      if (e->h_stage) cudaFreeHost(e->h_stage);
-      e->h_stage = nullptr;
-      e->h_cap = 0;
-      CK(cudaMallocHost(&e->h_stage, total * sizeof(ForceEntry)));
-      e->h_cap = total;
-    }
-    if (K > e->chunk_cap) {
-      for (int i = 0; i < n; ++i) {
-        if (e->d_ent[i]) cudaFree(e->d_ent[i]);
-        e->d_ent[i] = nullptr;
-        if (e->n_ent[i] > 0)
-          CK(cudaMalloc(&e->d_ent[i], (size_t)kEnsembleChunk * e->n_ent[i] * sizeof(ForceEntry)));
-      }
-      e->chunk_cap = kEnsembleChunk;
-      e->dirty = true;   // the entry pointers are baked into the graph
-    }
-    size_t off = 0;
-    for (int i = 0; i < n; ++i) {
-      if (e->n_ent[i] == 0) continue;
-      gt_handle* h = e->m[i];
-      std::vector<ForceEntry> steps;
-      for (int k = 0; k < K; ++k) {
-        const size_t before = steps.size();
-        draw_forcing(h->p, h->ht, seeds[i], steps);
-        if ((int)(steps.size() - before) != e->n_ent[i] ||
-            !entries_unique(steps.data() + before, steps.size() - before))
-          return GT_EINVAL;
-      }
-      std::memcpy(e->h_stage + off, steps.data(), steps.size() * sizeof(ForceEntry));
-      CK(cudaMemcpyAsync(e->d_ent[i], e->h_stage + off, steps.size() * sizeof(ForceEntry),
-                         cudaMemcpyHostToDevice, e->master));
-      off += steps.size();
-    }
-    CK(cudaMemsetAsync(e->d_step, 0, n * sizeof(int), e->master));
-    if (graph && K == kEnsembleChunk) {
-      // one graph launch advances every member by a whole chunk
-      if (e->dirty) {
-        const int rc = build_graph(e);
-        if (rc) return rc;
-      }
-      CK(cudaGraphLaunch(e->exec, e->master));
-    } else {
-      // one launch sequence per member and step, each member on its own stream
-      CK(cudaEventRecord(e->fork, e->master));
-      for (int i = 0; i < n; ++i) CK(cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0));
-      const std::vector<int> order = launch_order(e);
-      for (int k = 0; k < K; ++k)
-        for (int i : order) {
-          const int rc = member_enqueue(e, i);
-          if (rc) return rc;
-        }
-      for (int i = 0; i < n; ++i) {
-        CK(cudaEventRecord(e->join[i], e->m[i]->stream));
-        CK(cudaStreamWaitEvent(e->master, e->join[i], 0));
-      }
-    }
-    done += K;
-  }
-  CK(cudaStreamSynchronize(e->master));
-  for (auto h : e->m) {
-    const int rc = check_device_flag(h);
-    if (rc) return rc;
-  }
-  return GT_OK;
-}
 
 }  // extern "C"

@@ -1,5 +1,6 @@
 // Internal declarations shared by the host set-up code (gt_host.cpp), the
-// kernels (gt_kernels_impl.cuh, compiled once per precision) and the C-ABI (gt_capi.cu).
+// kernels (gt_kernels_impl.cuh, compiled once per precision) and the C-ABI
+// (gt_capi.cu, gt_autotune.cu, gt_tl_adj.cu, gt_ensemble.cu).
 #pragma once
 
 #include <cstddef>
