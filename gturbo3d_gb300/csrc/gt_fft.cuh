@@ -337,7 +337,9 @@ template <typename R, typename Idx> struct TripMem {
   }
 };
 
-template <int SIGN, typename R, int LGL, int LGNS, typename E, typename Mem, typename Sync>
+// PF: twiddles a stage ahead (FP32 default: measured faster); otherwise at
+// the stage itself (FP64: the extra live registers spill in the z pass).
+template <int SIGN, typename R, int LGL, int LGNS, bool PF, typename E, typename Mem, typename Sync>
 __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, const Mem& mem,
                                               const Sync& sync, const StageTw<R, LGL, LGNS>& cur) {
   constexpr int REM = LGL - LGNS;
@@ -345,9 +347,6 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
   constexpr bool LAST = (REM == LR);
   constexpr int NS = 1 << LGNS;
   constexpr int T = 1 << (LGL - 3);
-  // FP32: twiddles a stage ahead (measured faster); FP64: at the stage
-  // itself (the extra live registers spill in the FP64 z pass)
-  constexpr bool PF = sizeof(R) == 4;
   StageTw<R, LGL, LGNS + LR> nxt;
   if constexpr (!LAST && PF) nxt.load(t, tw);
   StageTw<R, LGL, LGNS> own;
@@ -401,7 +400,7 @@ __device__ __forceinline__ void fft_stages_ct(E v[8], int t, const Cplx<R>* __re
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = mem.ld(t + i * T);
     sync();
-    fft_stages_ct<SIGN, R, LGL, LGNS + LR>(v, t, tw, mem, sync, nxt);
+    fft_stages_ct<SIGN, R, LGL, LGNS + LR, PF>(v, t, tw, mem, sync, nxt);
   }
 }
 
@@ -423,14 +422,14 @@ template <int SIGN, typename R, int LGL, typename E, typename Idx, typename Sync
 __device__ __forceinline__ void fft_line_ct(E v[8], int t, const Cplx<R>* __restrict__ tw, E* sm,
                                             const Idx& idx, const Sync& sync = Sync{}) {
   const StageTw<R, LGL, 0> none{};
-  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, ArrMem<E, Idx>{sm, idx}, sync, none);
+  fft_stages_ct<SIGN, R, LGL, 0, sizeof(R) == 4>(v, t, tw, ArrMem<E, Idx>{sm, idx}, sync, none);
 }
 // The same with an explicit scratch policy (ArrMem, TripMem).
-template <int SIGN, typename R, int LGL, typename E, typename Mem, typename Sync>
+template <int SIGN, typename R, int LGL, bool PF = (sizeof(R) == 4), typename E, typename Mem, typename Sync>
 __device__ __forceinline__ void fft_line_mem(E v[8], int t, const Cplx<R>* __restrict__ tw, const Mem& mem,
                                              const Sync& sync) {
   const StageTw<R, LGL, 0> none{};
-  fft_stages_ct<SIGN, R, LGL, 0>(v, t, tw, mem, sync, none);
+  fft_stages_ct<SIGN, R, LGL, 0, PF>(v, t, tw, mem, sync, none);
 }
 
 // Strided shared-memory tile of a y or z pass: element e of column x of a

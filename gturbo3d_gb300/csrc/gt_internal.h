@@ -115,10 +115,12 @@ struct PipeMaps {
   int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
   int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
   int x_fused = 2;          // x pass: 2 = one thread group per row pair, a row's three lines
-                            // transformed together; 1 = the lines one by one; 0 = three
-                            // groups per row pair
+                            // transformed together; 3 = the same with row 0's products
+                            // parked in shared memory (the default for FP32 at NX = 512);
+                            // 1 = the lines one by one; 0 = three groups per row pair
   int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary
-  int z_split = 0;          // z inverse pass: 1 = curl part and k^2 part in separate kernels
+  int z_split = 0;          // z inverse pass: 1 = curl part and k^2 part in separate kernels;
+                            // 2 = one one-region kernel, inputs read again per output line
 };
 using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                      const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,

@@ -270,6 +270,93 @@ k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32
 }
 
 // ---------------------------------------------------------------------------
+// Pass 1 in one shared region: each of the six output lines (u = i k x a and
+// w = k^2 a) is formed from the input columns read again (after the first
+// read, from L2) instead of being parked in shared memory, so that a block
+// needs a third of the shared memory of k_zinv_curl and, with one or two
+// input fields live at a time, fewer registers: three resident blocks of 256
+// threads for FP32 instead of two.  Same columns, pruning and output, the
+// same expressions per element.
+// ---------------------------------------------------------------------------
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(kSpassThreads, sizeof(R) == 8 ? 2 : 3)
+k_zinv_curl1(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+  using C = Cplx<R>;
+  constexpr int W = zcols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
+  }
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  R kx[W], kxs[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const bool in = X0 + c < ylim;
+    kx[c] = in ? tb.fkx[X0 + c] : (R)0;
+    kxs[c] = in ? tb.fkxs[X0 + c] : (R)0;
+  }
+  const R ky = tb.fky[y], kys = tb.fkys[y];
+  E v[8];
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+    // the fields output f reads: u_0 <- (a1, a2), u_1 <- (a0, a2), u_2 <- (a0, a1); w_c <- a_c
+    const C* p1 = reinterpret_cast<const C*>(a.at(f < 3 ? (f == 0 ? 1 : 0) : f - 3));
+    const C* p2 = reinterpret_cast<const C*>(a.at(f == 2 ? 1 : 2));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+      const size_t o = (size_t)z * plane + base;
+      E q1 = load_cols<R, W>(p1, o, X0, lim);
+      E r;
+      if (f < 3) {
+        E q2 = load_cols<R, W>(p2, o, X0, lim);
+        const R kz = tb.fkz[z];
+#pragma unroll
+        for (int c = 0; c < W; ++c) {
+          const C b1 = col(q1, c), b2 = col(q2, c);
+          if (f == 0) {          // (py, pz) = (b1, b2)
+            col(r, c) = C{-ky * b2.y + kz * b1.y, ky * b2.x - kz * b1.x};
+          } else if (f == 1) {   // (px, pz) = (b1, b2)
+            col(r, c) = C{-kz * b1.y + kx[c] * b2.y, kz * b1.x - kx[c] * b2.x};
+          } else {               // (px, py) = (b1, b2)
+            col(r, c) = C{-kx[c] * b2.y + ky * b1.y, kx[c] * b2.x - ky * b1.x};
+          }
+        }
+      } else {
+        const R kzs = tb.fkzs[z];
+#pragma unroll
+        for (int c = 0; c < W; ++c) {
+          const R k2 = (kxs[c] + kys) + kzs;
+          const C qq = col(q1, c);
+          col(r, c) = C{k2 * qq.x, k2 * qq.y};
+        }
+      }
+      v[i] = r;
+    }
+    // the previous line's last reads of sm precede the final barrier of its
+    // transform, so the scratch is free again here
+    fft_line_ct<+1, R, LGZ>(v, t, tw, sm, idx);
+    C* out = reinterpret_cast<C*>(w.at(f));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Strided (y or z) transform of up to six fields, in place.  blockIdx.z picks
 // the field, blockIdx.y the outer index (z for a y pass, y for a z pass).
 // ---------------------------------------------------------------------------
@@ -580,8 +667,10 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 // ---------------------------------------------------------------------------
 template <typename R> constexpr int xbatch_threads() { return sizeof(R) == 8 ? 128 : 256; }
 
-template <typename R, int LGN>
-__global__ void __launch_bounds__(xbatch_threads<R>(), 2)
+// PARK: row 0's products wait in a shared region (N complex + N real per
+// group) instead of registers, for 3 resident blocks instead of 2.
+template <typename R, int LGN, bool PARK = false>
+__global__ void __launch_bounds__(xbatch_threads<R>(), PARK ? 3 : 2)
 k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
   using C = Cplx<R>;
   using E = CTrip<R>;
@@ -596,8 +685,10 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
   C* lines = sm + (size_t)grp * 3 * LP;
   const TripMem<R, SwzIdx> mem{lines, SwzIdx{0}, LP};
   E v[8];
-  C a0[8];
-  R cz0[8];
+  C a0[PARK ? 1 : 8];
+  R cz0[PARK ? 1 : 8];
+  C* park_a = sm + (size_t)3 * P * LP + (size_t)grp * LP;
+  R* park_z = reinterpret_cast<R*>(sm + (size_t)4 * P * LP) + (size_t)grp * LP;
   auto run = [&](auto sync) {
 #pragma unroll 1
     for (int r = 0; r < 2; ++r) {
@@ -612,7 +703,7 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
         v[i].c = pack_c2r<R>(reinterpret_cast<const C*>(w.p[4]) + row * nhp,
                              reinterpret_cast<const C*>(w.p[5]) + row * nhp, e, N, xa);
       }
-      fft_line_mem<+1, R, LGN>(v, t, tw, mem, sync);
+      fft_line_mem<+1, R, LGN, (sizeof(R) == 4 && !PARK)>(v, t, tw, mem, sync);
       // u = (z0.x, z0.y, z1.x), w = (z1.y, z2.x, z2.y) (produ.f90:14-16)
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
@@ -620,7 +711,15 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
         const R cx = z0.y * z2.y - z1.x * z2.x;
         const R cy = z1.x * z1.y - z0.x * z2.y;
         const R cz = z0.x * z2.x - z0.y * z1.y;
-        if (r == 0) {
+        if constexpr (PARK) {
+          const int e = t + i * T;   // each thread reads back only its own positions
+          if (r == 0) {
+            park_a[e] = C{cx, cy};
+            park_z[e] = cz;
+          } else {
+            v[i] = E{park_a[e], C{cx, cy}, C{park_z[e], cz}};
+          }
+        } else if (r == 0) {
           a0[i] = C{cx, cy};
           cz0[i] = cz;
         } else {
@@ -629,7 +728,7 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
       }
     }
     // forward: planes 0, 1, 2 = c_x + i c_y of rows 0 and 1, c_z(0) + i c_z(1)
-    fft_line_mem<-1, R, LGN>(v, t, tw, mem, sync);
+    fft_line_mem<-1, R, LGN, (sizeof(R) == 4 && !PARK)>(v, t, tw, mem, sync);
 #pragma unroll
     for (int i = 0; i < 8; ++i) mem.st(t + i * T, v[i]);
     sync();
@@ -1340,11 +1439,12 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 12 + 1];
+  cudaError_t es[8 * 14 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
   es[n++] = allow_smem(k_zk2<R, LG>, optin);             \
+  es[n++] = allow_smem(k_zinv_curl1<R, LG>, optin);      \
   es[n++] = allow_smem(k_spass<R, 1, LG>, optin);        \
   es[n++] = allow_smem(k_spass<R, -1, LG>, optin);       \
   if (sizeof(R) == 4) {                                  \
@@ -1353,6 +1453,7 @@ static int set_smem_attrs() {
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
+  es[n++] = allow_smem(k_xbatch<R, LG, true>, optin);    \
   es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
   es[n++] = allow_smem(k_zfwd_zinv<R, LG>, optin);       \
   es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
@@ -1456,12 +1557,22 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
     GT_HOOK(kKZinvCurl, true);
-    const int split = pm && pm->z_split && c.threads / zcols<R>() <= kSpassThreads ? 1 : 0;
+    const bool fits = c.threads / zcols<R>() <= kSpassThreads;
+    const int split = pm && pm->z_split == 1 && fits ? 1 : 0;
+    if (pm && pm->z_split == 2 && fits) {
+      // one shared region, the input columns read again per output line
+#define GT_L(LG)                                                                                   \
+  k_zinv_curl1<R, LG><<<grid, c.threads / zcols<R>(), c.smem / 3, s>>>(pa, pw, tb, g, c.lgTX, pruned, \
+                                                                       tb.ztl[c.lgTX]);
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else {
 #define GT_L(LG)                                                                                   \
   k_zinv_curl<R, LG><<<grid, c.threads / zcols<R>(), c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned,    \
                                                                   tb.ztl[c.lgTX], split ? 0 : 1);
-    GT_DISPATCH_LG(g.lnz, GT_L)
+      GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
+    }
     if (split && !(rc = (int)cudaGetLastError())) {
       // w = k^2 a: one field per block, one shared region (a third of the smem)
       const dim3 grid2 = pruned ? dim3(tb.nztl[c.lgTX], 3) : dim3(c.ntiles, 3, g.ny);
@@ -1510,6 +1621,13 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       GT_HOOK(kKXCross, true);
       if (!pm || pm->x_fused == 2) {
 #define GT_L(LG) k_xbatch<R, LG><<<(unsigned)(npairs / P), P * T, 3 * smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+        GT_DISPATCH_LG(gs.lnx, GT_L)
+#undef GT_L
+      } else if (pm->x_fused == 3) {
+        // three planes and the parking region (N complex + N real per group)
+        const int psmem = 3 * smem + smem + smem / 2;
+#define GT_L(LG) \
+  k_xbatch<R, LG, true><<<(unsigned)(npairs / P), P * T, psmem, s>>>(pw, gs, tb.twx, shalf, xlim);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       } else {

@@ -188,12 +188,16 @@ int gt_set_pipelining(gt_handle* h, int32_t enable);
  * "pipe_y", "pipe_z", "pipe_x" (0/1: TMA-pipelined persistent pass or one tile per block),
  * "x_pairs" (row pairs per pipelined x-pass block, 1..8), "x_stages" (2..4),
  * "x_fused" (x pass: 2 = one thread group per row pair, the three packed lines
- * of a row transformed together, u x w in registers (default); 1 = the same
- * with the lines transformed one by one; 0 = three groups per row pair), "y_pairs" (0/1: FP32 y passes with
+ * of a row transformed together, u x w in registers (default); 3 = the same
+ * with row 0's products parked in shared memory, three resident blocks per SM
+ * (the default for the mixed form at NX = 512);
+ * 1 = the lines transformed one by one; 0 = three groups per row pair),
+ * "y_pairs" (0/1: FP32 y passes with
  * two adjacent columns per thread, or one), "fuse_stage" (0/1: the first nonlinear
  * term's z forward pass and the second term's z inverse pass as one kernel that
- * keeps the stage value c on chip, or two passes with c in HBM), "z_split" (0/1:
- * the z inverse pass's w = k^2 a in its own one-region kernel). */
+ * keeps the stage value c on chip, or two passes with c in HBM), "z_split" (z inverse
+ * pass: 0 = one three-region kernel; 1 = w = k^2 a in its own one-region kernel;
+ * 2 = one one-region kernel that reads the input columns again per output line). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 
 /* Allocation-free kinetic energy, for callers that cannot allocate device

@@ -78,11 +78,12 @@ def test_pipelined_passes_equal_plain(lib, n, precision, tol, truncate):
                                              ((8, 16, 16), "fp64", 1e-13), ((16, 32, 8), "mixed", 1e-5),
                                              ((1024, 8, 8), "mixed", 1e-5), ((1024, 8, 8), "fp64", 1e-13)])
 @pytest.mark.parametrize("truncate", [1, 0])
-@pytest.mark.parametrize("fused", [1, 2])
+@pytest.mark.parametrize("fused", [1, 2, 3])
 def test_fused_x_pass_equals_three_group_pass(lib, n, precision, tol, truncate, fused):
     """The register-resident x pass (one thread group per row pair; 2: its
-    three lines per row transformed together) and the three-group x pass
-    compute the same u x w and give the same step."""
+    three lines per row transformed together; 3: the same with row 0's
+    products parked in shared memory) and the three-group x pass compute the
+    same u x w and give the same step."""
     import gturbo3d_gb300 as g
     gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate)
     gp.famp = g.forcing_amplitude(0.1, gp)
@@ -165,9 +166,11 @@ def test_fused_stage_boundary_equals_separate_passes(lib, n, precision, tol, tru
 @pytest.mark.parametrize("n,precision,tol", [(32, "fp64", 1e-14), (64, "mixed", 1e-6), ((16, 64, 32), "mixed", 1e-6),
                                              ((64, 16, 1024), "fp64", 1e-14), ((8, 8, 16), "mixed", 1e-6)])
 @pytest.mark.parametrize("truncate", [1, 0])
-def test_split_z_inverse_equals_combined(lib, n, precision, tol, truncate):
-    """The z inverse pass with w = k^2 a in its own one-region kernel gives the
-    result of the combined three-region kernel."""
+@pytest.mark.parametrize("split", [1, 2])
+def test_split_z_inverse_equals_combined(lib, n, precision, tol, truncate, split):
+    """The z inverse pass with w = k^2 a in its own one-region kernel (1), or
+    as one one-region kernel that reads its input columns again per output
+    line (2), gives the result of the combined three-region kernel."""
     import gturbo3d_gb300 as g
     gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate)
     gp.famp = g.forcing_amplitude(0.1, gp)
@@ -175,7 +178,7 @@ def test_split_z_inverse_equals_combined(lib, n, precision, tol, truncate):
     with g.Simulation(gp) as a, g.Simulation(gp) as b:
         a.set_state(b0)
         b.set_state(b0)
-        a.set_tuning("z_split", 1)
+        a.set_tuning("z_split", split)
         b.set_tuning("z_split", 0)
         a.step(3, 5)
         b.step(3, 5)
