@@ -14,6 +14,9 @@ both integrating-factor updates and the forcing.
              each step and the energy (gt_energy) read back each step
   fp64       the plain FP64 form's steps/s on the same workload
   rel_energy_err  |E_mixed - E_fp64| / E_fp64 after --energy-steps steps
+  gpu_reference_style  the reference's unfused routine sequence with cuFFT
+             (torch.fft) on the same GPU, FP64 and FP32 steps/s, and its FP64
+             trajectory's difference from the library's (--cufft-steps)
 
 The working set (12 fields, 6.6 GB mixed / 13 GB FP64) is far larger than the
 129 MB L2, so no flush is needed between steps.
@@ -233,6 +236,140 @@ def time_e2e(sim, steps, seed, torch):
     return dt, np.array(e), s
 
 
+class CufftStep:
+    """The reference-style GPU baseline: one RK2 step as the reference's
+    unfused routine sequence (main.f90:121-150) with cuFFT through torch.fft
+    and one array operation per routine: curl, k^2 scale, six C2R transforms,
+    cross, three R2C transforms, Coriolis, invcurl and trunc (nlt.f90:16-89),
+    step1, the second nlt, step2 (rkstep.f90:30-48, 86-104) and the forcing
+    adds (drawn by the library's host LCG ahead of time).  A measured comparison only: none of
+    the library's kernels runs in it."""
+
+    def __init__(self, p, torch, real_dtype, device=None):
+        t = torch
+        self.t, self.p, self.rd = t, p, real_dtype
+        nx, ny, nz = p.nx, p.ny, p.nz
+        nh = nx // 2 + 1
+        self.shape = (nz, ny, nx)
+        dev = device if device is not None else t.device("cuda", t.cuda.current_device())
+        self.dev = dev
+
+        def freq(n, xl):   # defk.f90:29-43: j for j <= n/2, j - n above
+            j = t.arange(n, dtype=t.float64, device=dev)
+            return t.where(j <= n // 2, j, j - n) * (2.0 * math.pi / xl)
+
+        kx = t.arange(nh, dtype=t.float64, device=dev) * (2.0 * math.pi / p.xlx)
+        ky, kz = freq(ny, p.xly), freq(nz, p.xlz)
+        k2 = (kx[None, None, :] ** 2 + ky[None, :, None] ** 2) + kz[:, None, None] ** 2
+        scra = p.nu * k2.pow(p.alpnu) + p.mu * k2.pow(p.alpmu)
+        emk = t.exp((-0.5 * p.dt) * scra)
+        emk[0, 0, 0] = 1.0
+        m = ((kz[:, None, None] ** 2 / kz[nz // 2] ** 2 + ky[None, :, None] ** 2 / ky[ny // 2] ** 2)
+             + kx[None, None, :] ** 2 / kx[nh - 1] ** 2) > p.rtrunc * p.rtrunc
+        m = m.expand(nz, ny, nh).clone()
+        m[0, 0, 0] = True
+        ik2 = t.where(k2 > 0, 1.0 / t.where(k2 > 0, k2, t.ones_like(k2)), t.zeros_like(k2))
+        self.kx, self.ky, self.kz = (v.to(real_dtype) for v in (kx[None, None, :], ky[None, :, None],
+                                                               kz[:, None, None]))
+        self.k2, self.emk, self.ik2 = k2.to(real_dtype), emk.to(real_dtype), ik2.to(real_dtype)
+        self.keep = (~m).to(real_dtype) if p.truncate == 1 else None
+        self.dt2 = 0.5 * p.dt if p.dt2_mode == 1 else 0.0
+
+    def cross_k(self, a, scale=None):
+        """i k x a (optionally times scale)."""
+        kx, ky, kz = self.kx, self.ky, self.kz
+        if scale is not None:
+            kx, ky, kz = kx * scale, ky * scale, kz * scale
+        return [1j * (ky * a[2] - kz * a[1]), 1j * (kz * a[0] - kx * a[2]), 1j * (kx * a[1] - ky * a[0])]
+
+    def nlt(self, a, bcor):
+        t = self.t
+        v = self.cross_k(a)                                          # curl
+        w = [self.k2 * a[c] for c in range(3)]                       # k^2 scale
+        ur = [t.fft.irfftn(x, s=self.shape, dim=(0, 1, 2), norm="forward") for x in v]
+        wr = [t.fft.irfftn(x, s=self.shape, dim=(0, 1, 2), norm="forward") for x in w]
+        cr = [ur[1] * wr[2] - ur[2] * wr[1], ur[2] * wr[0] - ur[0] * wr[2], ur[0] * wr[1] - ur[1] * wr[0]]
+        vh = [t.fft.rfftn(x, dim=(0, 1, 2), norm="forward") for x in cr]
+        okz = self.p.omega * self.kz
+        out = [vh[c] + 1j * okz * bcor[c] for c in range(3)]         # Coriolis
+        res = self.cross_k(out, self.ik2)                            # invcurl
+        for c in range(3):
+            res[c][0, 0, 0] = out[c][0, 0, 0]
+            if self.keep is not None:                                # trunc
+                res[c] = res[c] * self.keep
+        return res
+
+    def draw(self, seed, nsteps):
+        """The forcing adds of nsteps steps, drawn on the host before timing
+        (the host call enumerates the forced modes afresh each time, which
+        the library's handle does once); returns (per-step adds, new seed)."""
+        import gturbo3d_gb300 as g
+        out = []
+        for _ in range(nsteps):
+            ix, iy, iz, dF, seed = g.forcing_increments(self.p, seed)
+            t = self.t
+            idx = tuple(t.as_tensor(v, device=self.dev).long() for v in (iz, iy, ix))
+            out.append((idx, t.as_tensor(dF, device=self.dev).to(self.rd)) if len(ix) else None)
+        return out, seed
+
+    def step(self, b, adds):
+        n1 = self.nlt(b, b)
+        c = [self.emk * (b[i] + self.dt2 * n1[i]) for i in range(3)]          # step1
+        for x in c:
+            x[0, 0, 0] = 0
+        n2 = self.nlt(c, b)
+        bn = [self.emk * (self.emk * b[i] + self.p.dt * n2[i]) for i in range(3)]   # step2
+        for x in bn:
+            x[0, 0, 0] = 0
+        if adds is not None:
+            idx, d = adds
+            for i in range(3):   # (Re, Im) pairs added in place, repeated modes accumulated
+                self.t.view_as_real(bn[i]).index_put_(idx, d[:, 2 * i:2 * i + 2], accumulate=True)
+        return bn
+
+
+def cufft_baseline(b0, seed, device, steps, torch):
+    """Steps/s of CufftStep at 512^3 in FP64 and FP32 (CUDA events on torch's
+    stream, one untimed warm-up step for the cuFFT plans, forcing adds drawn
+    before the timed steps), and the FP64 trajectory's relative L2 difference
+    from the library's FP64 step after the same steps."""
+    import numpy as np
+    import gturbo3d_gb300 as g
+    out = {"impl": "torch.fft (cuFFT) + torch elementwise ops, one op per reference routine, unfused",
+           "steps": steps}
+    for name, rd, cd in (("fp64", torch.float64, torch.complex128), ("fp32", torch.float32, torch.complex64)):
+        try:
+            p = g.make_params(N, precision="fp64", forcing="3d3c", device=device, **PHYS)
+            p.famp = g.forcing_amplitude(INJECTION, p)
+            st = CufftStep(p, torch, rd)
+            b = [torch.as_tensor(x, device=st.dev).to(cd) for x in b0]
+            adds, _ = st.draw(seed, steps + 1)
+            b = st.step(b, adds[0])
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for k in range(steps):
+                b = st.step(b, adds[k + 1])
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            out[name] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms}
+            if name == "fp64":
+                with g.Simulation(p) as ref:
+                    ref.set_state(b0)
+                    ref.step(steps + 1, seed)
+                    lb = ref.get_state()
+                num = sum(float(np.sum(np.abs(b[i].cpu().numpy() - lb[i]) ** 2)) for i in range(3))
+                den = sum(float(np.sum(np.abs(lb[i]) ** 2)) for i in range(3))
+                out["fp64"]["rel_l2_diff_vs_library_fp64"] = math.sqrt(num / den)
+            del st, b
+            torch.cuda.empty_cache()
+        except Exception as ex:   # a reported comparison, not the measurement
+            out[name] = {"error": str(ex)[:200]}
+    return out
+
+
 def _oracle_step_time(n, cores):
     """Seconds of one FP64 oracle RK2 step (slab-parallel pointwise work,
     scipy.fft on every core) at n^3, and the sample description."""
@@ -414,6 +551,8 @@ def run_ours(args):
             "rel_energy_err_mixed_vs_fp64": rel_err, "energy_steps": args.energy_steps,
             "roofline": roof, "clocks": clk}
     sim.close()
+    if rank == 0 and args.cufft_steps > 0:
+        line["gpu_reference_style"] = cufft_baseline(b0, seed, device, args.cufft_steps, torch)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -618,6 +757,8 @@ def main():
     ap.add_argument("--energy-steps", type=int, default=100)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cufft-steps", type=int, default=3,
+                    help="timed steps of the reference-style cuFFT (torch.fft) GPU baseline; 0 skips it")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer timing (profiling runs)")
     ap.add_argument("--size", type=int, default=512,
                     help="grid size (512 default; 1024 runs the roofline sweep's second size with nu = 8e-5)")
