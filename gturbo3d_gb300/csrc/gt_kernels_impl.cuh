@@ -9,12 +9,13 @@
 //                     the inverse z transform of all six fields.
 //   2. k_spass2     : inverse y transform of the six fields, in place (FP32,
 //                     two columns per thread; k_spass for FP64).
-//   3. k_xfused     : per pair of (y,z) rows, the six C2R x transforms (two
-//                     fields per complex FFT), u x w in registers
+//   3. k_xbatch     : per pair of (y,z) rows, the six C2R x transforms (two
+//                     fields per complex FFT, a row's three packed lines as
+//                     one three-line transform), u x w in registers
 //                     (produ.f90:9-28), the three R2C x transforms and the
 //                     1/(NX NY NZ) scaling (fft_dir.f90:17-25); real space
-//                     never reaches HBM (k_xcross: the same with three
-//                     thread groups per row pair).
+//                     never reaches HBM (k_xfused: the lines one by one;
+//                     k_xcross: three thread groups per row pair).
 //   4. k_spass2     : forward y transform of the three fields.
 //   5. k_zfwd_epi   : forward z transform, then per mode the Coriolis term
 //                     (nlt.f90:67-81), invcurl (produ.f90:79-101), trunc
