@@ -58,6 +58,7 @@ SIGNATURES = {
     "gt_rann": (C.c_int, [_ip, C.c_int32, _P(C.c_float)]),
     "gt_forced_modes": (C.c_int, [_P(GtParams), _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "gt_forcing_increments": (C.c_int, [_P(GtParams), _ip, C.c_int32, _ip, _ip, _ip, _ip, _dp]),
+    "gt_init_noise": (C.c_int, [_P(GtParams), _ip, _dp, _dp, _dp]),
     "gt_seed_read": (C.c_int, [C.c_char_p, _ip]),
     "gt_seed_write": (C.c_int, [C.c_char_p, C.c_int32]),
     "gt_field_read_f32": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, _P(C.c_float)]),

@@ -123,6 +123,18 @@ def forcing_increments(p: GtParams, seed: int):
     return ix[:m].copy(), iy[:m].copy(), iz[:m].copy(), dF[:m].copy(), s.value
 
 
+def init_noise(p: GtParams, seed: int):
+    """The reference's fresh-start noise (trunc.f90:75-93): returns the three
+    physical components (double[NZ][NY][NX], sqrt(dt) (rann - 0.5) each) and
+    the advanced seed; Simulation.set_state_physical turns them into the
+    initial state (main.f90:91-106)."""
+    lib = load()
+    u = [np.zeros((p.nz, p.ny, p.nx)) for _ in range(3)]
+    s = C.c_int32(seed)
+    check(lib.gt_init_noise(C.byref(p), C.byref(s), _dp(u[0]), _dp(u[1]), _dp(u[2])), "gt_init_noise")
+    return u, s.value
+
+
 def forcing_amplitude(injection: float, p: GtParams) -> float:
     """famp giving the mean energy input nf famp^2 = injection (iniforcing_3d3c.f90:39)."""
     nf = forced_modes(p).nf

@@ -1,9 +1,10 @@
 // Host-side set-up: wavenumber tables and integrating factor (defk.f90),
 // forced-mode enumeration (iniforcing_3d3c.f90 / iniforcing_2d2c.f90), the
 // reference RNG and forcing draws (forcing_3d3c.f90 / forcing_2d2c.f90),
-// params.dat parsing (inieuler.f90:14-20), seed and field files
-// (main.f90:37-45, read.f90, write.f90).  No CUDA here: everything in this
-// file runs without a GPU.
+// the initial noise (trunc.f90:75-93), params.dat parsing
+// (inieuler.f90:14-20), seed and field files (main.f90:37-45, read.f90,
+// write.f90).  No CUDA here: everything in this file runs without a GPU.
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -11,7 +12,9 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <thread>
 #include <unordered_set>
+#include <vector>
 
 #include "gt_internal.h"
 
@@ -152,6 +155,61 @@ float rann(int32_t& irand) {
   x = x * (uint32_t)kLcgMul + 1u;
   irand = (int32_t)(x & (uint32_t)kLcgMask);
   return (float)((double)irand / (double)kLcgMask);
+}
+
+// The LCG step x -> (69069 x + 1) mod 2^31 applied m times is the affine map
+// x -> (am x + cm) mod 2^31; composing maps by squaring gives (am, cm) in
+// log2 m steps, so that threads can start at any position of the stream.
+static void lcg_jump(uint64_t m, uint32_t& am, uint32_t& cm) {
+  uint32_t a = 1u, c = 0u;                          // accumulated map
+  uint32_t pa = (uint32_t)kLcgMul, pc = 1u;         // the map of 2^bit steps
+  while (m) {
+    if (m & 1u) {                                   // accumulated after (pa, pc)
+      c = (pa * c + pc) & (uint32_t)kLcgMask;
+      a = (pa * a) & (uint32_t)kLcgMask;
+    }
+    pc = (pa * pc + pc) & (uint32_t)kLcgMask;
+    pa = (pa * pa) & (uint32_t)kLcgMask;
+    m >>= 1;
+  }
+  am = a;
+  cm = c;
+}
+
+void init_noise(const gt_params& p, int32_t& seed, double* ux, double* uy, double* uz) {
+  // trunc.f90:75-93: for k, j, i: b{x,y,z}(i,j,k) += sdt*(rann(seed)-0.5),
+  // the three components of a point drawn in turn; rann - 0.5 is REAL*4
+  // arithmetic, promoted to REAL*8 by the product with sdt = sqrt(dt)
+  // (inieuler.f90:67).  The arrays start at zero (inieuler.f90:79-81), so the
+  // result is the noise itself.
+  const double sdt = std::sqrt(p.dt);
+  const size_t npts = (size_t)p.nx * p.ny * p.nz;
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  if (nt > 64) nt = 64;
+  if (npts < (size_t)nt * 65536) nt = 1;
+  const uint32_t x0 = (uint32_t)seed & (uint32_t)kLcgMask;
+  auto work = [&](size_t p0, size_t p1) {
+    uint32_t am, cm;
+    lcg_jump(3ull * p0, am, cm);
+    int32_t irand = (int32_t)((am * x0 + cm) & (uint32_t)kLcgMask);
+    for (size_t q = p0; q < p1; ++q) {
+      ux[q] = sdt * (double)(rann(irand) - 0.5f);
+      uy[q] = sdt * (double)(rann(irand) - 0.5f);
+      uz[q] = sdt * (double)(rann(irand) - 0.5f);
+    }
+  };
+  std::vector<std::thread> pool;
+  const size_t chunk = (npts + nt - 1) / nt;
+  for (unsigned i = 1; i < nt; ++i) {
+    const size_t p0 = i * chunk, p1 = std::min(npts, p0 + chunk);
+    if (p0 < p1) pool.emplace_back(work, p0, p1);
+  }
+  work(0, std::min(npts, chunk));
+  for (auto& th : pool) th.join();
+  uint32_t am, cm;
+  lcg_jump(3ull * npts, am, cm);
+  seed = (int32_t)((am * x0 + cm) & (uint32_t)kLcgMask);
 }
 
 void draw_forcing(const gt_params& p, const HostTables& t, int32_t& seed,
@@ -340,6 +398,14 @@ int gt_memory_estimate(const gt_params* p, size_t* bytes) {
 int gt_rann(int32_t* irand, int32_t n, float* out) {
   if (!irand || n < 0 || (n > 0 && !out)) return GT_EINVAL;
   for (int32_t i = 0; i < n; ++i) out[i] = rann(*irand);
+  return GT_OK;
+}
+
+int gt_init_noise(const gt_params* p, int32_t* seed, double* ux, double* uy, double* uz) {
+  if (!p || !seed || !ux || !uy || !uz) return GT_EINVAL;
+  const int rc = gt_params_validate(p);
+  if (rc) return rc;
+  gt::init_noise(*p, *seed, ux, uy, uz);
   return GT_OK;
 }
 

@@ -112,6 +112,13 @@ int gt_forced_modes(const gt_params* p, int32_t* nf, int32_t* ix, int32_t* iy, i
  * Feed them to gt_rk2_step_coeffs for host-driven forcing. */
 int gt_forcing_increments(const gt_params* p, int32_t* seed, int32_t cap, int32_t* n,
                           int32_t* ix, int32_t* iy, int32_t* iz, double* dF);
+/* The reference's initial noise for a fresh start (inieuler.f90:76-82,
+ * trunc.f90:75-93): u_c = sqrt(dt) * (rann(seed) - 0.5) at every point, the
+ * three components of a point drawn in turn, points in Fortran order (x
+ * fastest), REAL*4 difference promoted to REAL*8.  Writes double[NZ][NY][NX]
+ * each and advances *seed by 3 NX NY NZ draws; feed the result to
+ * gt_set_state_physical (main.f90:91-106).  Host only. */
+int gt_init_noise(const gt_params* p, int32_t* seed, double* ux, double* uy, double* uz);
 /* Reads / writes the seed file files/seed.NNN (main.f90:40-45, 207-210). */
 int gt_seed_read(const char* path, int32_t* seed);
 int gt_seed_write(const char* path, int32_t seed);

@@ -765,6 +765,19 @@ def incompr(a, wk):
     return out, cc
 
 
+def init_noise(p: Params, seed: int):
+    """The fresh-start noise (inieuler.f90:76-82, trunc.f90:75-93): the arrays
+    start at zero and, for k, j, i (x fastest), b{x,y,z}(i,j,k) +=
+    sdt*(rann(seed)-0.5) with the three components drawn in turn; rann - 0.5
+    is REAL*4 arithmetic, promoted by the REAL*8 sdt = sqrt(dt)
+    (inieuler.f90:67).  Returns ([ux, uy, uz] as float64[NZ, NY, NX], seed)."""
+    n = p.nx * p.ny * p.nz
+    r, seed = rann_stream(seed, 3 * n)
+    d = (r - np.float32(0.5)).astype(np.float32).reshape(n, 3)
+    sdt = math.sqrt(p.dt)
+    return [sdt * d[:, c].astype(np.float64).reshape(p.nz, p.ny, p.nx) for c in range(3)], seed
+
+
 def velocity_to_potential(ur, p, wk, mask=None):
     """main.f90:91-106: fft_dir x3, incompr, invcurl, trunc x3."""
     a = [fft_dir(ur[c], p) for c in range(3)]

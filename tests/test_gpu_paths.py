@@ -36,6 +36,25 @@ def test_initial_state_path(lib, precision, tol):
     assert abs(cc - cc_ref) / cc_ref < max(tol, 1e-12) * 10
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+def test_fresh_start_from_reference_noise(lib, precision, tol):
+    """The reference's fresh start (inieuler.f90:76-82): the host noise of
+    gt_init_noise through the device initial-state path equals the oracle's
+    init_noise through its velocity_to_potential."""
+    import gturbo3d_gb300 as g
+    from oracle.gturbo_oracle import Oracle, init_noise, velocity_to_potential
+    gp, op = configs(32, precision=precision, forcing="none")
+    u, seed = g.init_noise(gp, 8299396)
+    ou, oseed = init_noise(op, 8299396)
+    assert seed == oseed and all(np.array_equal(u[c], ou[c]) for c in range(3))
+    ref, cc_ref = velocity_to_potential(ou, op, Oracle(op).wk)
+    with g.Simulation(gp) as sim:
+        cc = sim.set_state_physical(u)
+        got = sim.get_state()
+    assert relerr(got, ref) < tol
+    assert abs(cc - cc_ref) / cc_ref < max(tol, 1e-12) * 10
+
+
 @pytest.mark.gpu
 def test_bounded_wait_times_out_and_handle_survives(lib):
     """A device wait that nothing completes gives up, reports GT_ETIMEOUT
