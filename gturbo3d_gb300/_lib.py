@@ -61,6 +61,8 @@ SIGNATURES = {
     "gt_init_noise": (C.c_int, [_P(GtParams), _ip, _dp, _dp, _dp]),
     "gt_seed_read": (C.c_int, [C.c_char_p, _ip]),
     "gt_seed_write": (C.c_int, [C.c_char_p, C.c_int32]),
+    "gt_frame_read": (C.c_int, [C.c_char_p, _ip, _dp]),
+    "gt_frame_write": (C.c_int, [C.c_char_p, C.c_int32, C.c_double]),
     "gt_field_read_f32": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, _P(C.c_float)]),
     "gt_field_write_f32": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, _P(C.c_float)]),
     "gt_create": (C.c_int, [_P(GtParams), _P(_vp)]),

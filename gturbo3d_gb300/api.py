@@ -151,6 +151,17 @@ def write_seed(path: str, seed: int) -> None:
     check(load().gt_seed_write(str(path).encode(), seed), "gt_seed_write")
 
 
+def read_frame(path: str) -> tuple[int, float]:
+    """curframe.dat: (ifr, t) a continuation starts from (main.f90:37-39)."""
+    f, t = C.c_int32(), C.c_double()
+    check(load().gt_frame_read(str(path).encode(), C.byref(f), C.byref(t)), "gt_frame_read")
+    return f.value, t.value
+
+
+def write_frame(path: str, ifr: int, t: float) -> None:
+    check(load().gt_frame_write(str(path).encode(), ifr, t), "gt_frame_write")
+
+
 def read_field(path: str, nx: int, ny: int, nz: int) -> np.ndarray:
     """One float32 velocity component, fields/u?.NNN (read.f90:12-22)."""
     out = np.zeros((nz, ny, nx), np.float32)

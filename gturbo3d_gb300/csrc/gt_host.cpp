@@ -475,6 +475,32 @@ int gt_seed_write(const char* path, int32_t seed) {
   return ok ? GT_OK : GT_EIO;
 }
 
+int gt_frame_read(const char* path, int32_t* ifr, double* t) {
+  // main.f90:37-39: read(1,*) ifr, t
+  if (!path || !ifr || !t) return GT_EINVAL;
+  std::ifstream in(path);
+  if (!in) return GT_EIO;
+  std::vector<std::string> v;
+  if (!read_values(in, 2, v)) return GT_EIO;
+  int32_t f;
+  double tt;
+  if (!to_int(v[0], f) || !to_double(v[1], tt)) return GT_EIO;
+  *ifr = f;
+  *t = tt;
+  return GT_OK;
+}
+
+int gt_frame_write(const char* path, int32_t ifr, double t) {
+  // main.f90:213-215: write(1,*) ifr, t (list-directed; 17 significant digits
+  // read back exactly)
+  if (!path) return GT_EINVAL;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return GT_EIO;
+  int ok = std::fprintf(f, " %12d %25.17E\n", ifr, t) > 0;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? GT_OK : GT_EIO;
+}
+
 // Fortran unformatted sequential records: a 4-byte length marker before and
 // after the data.  Records longer than 2^31-1 bytes are split into
 // sub-records whose leading marker is negative while more follow (the

@@ -122,6 +122,10 @@ int gt_init_noise(const gt_params* p, int32_t* seed, double* ux, double* uy, dou
 /* Reads / writes the seed file files/seed.NNN (main.f90:40-45, 207-210). */
 int gt_seed_read(const char* path, int32_t* seed);
 int gt_seed_write(const char* path, int32_t seed);
+/* Reads / writes curframe.dat, the frame number and time a continuation
+ * starts from (main.f90:37-39, 212-215).  Host only. */
+int gt_frame_read(const char* path, int32_t* ifr, double* t);
+int gt_frame_write(const char* path, int32_t ifr, double t);
 /* Reads / writes one float32 real-space field as a Fortran unformatted
  * sequential record of NX*NY*NZ values, x fastest (read.f90:12-52,
  * write.f90:12-22). */

@@ -149,6 +149,29 @@ def test_seed_and_field_files_round_trip(lib, tmp_path):
     assert np.array_equal(g.read_field(str(tmp_path / "ux.001"), 32, 16, 8), u)
 
 
+def test_curframe_round_trip_and_reference_forms(lib, tmp_path):
+    """curframe.dat (main.f90:37-39, 212-215): what gt_frame_write writes
+    reads back exactly; list-directed forms a Fortran write or an edited file
+    holds (blanks, a comma, a 'd' exponent) read too; a missing or short file
+    is GT_EIO."""
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300 import _lib
+    f = tmp_path / "curframe.dat"
+    g.write_frame(str(f), 7, 0.1 + 0.2)
+    assert g.read_frame(str(f)) == (7, 0.1 + 0.2)
+    for text, want in [("           3   1.5000000000000000     \n", (3, 1.5)),
+                       ("12, 2.5d-1\n", (12, 0.25)), ("0 0.d0\n", (0, 0.0))]:
+        f.write_text(text)
+        assert g.read_frame(str(f)) == want
+    f.write_text("4\n")
+    with pytest.raises(_lib.GturboError) as ei:
+        g.read_frame(str(f))
+    assert ei.value.code == _lib.GT_EIO
+    with pytest.raises(_lib.GturboError) as ei:
+        g.read_frame(str(tmp_path / "missing.dat"))
+    assert ei.value.code == _lib.GT_EIO
+
+
 def test_field_file_errors(lib, tmp_path):
     import gturbo3d_gb300 as g
     from gturbo3d_gb300 import _lib
