@@ -467,7 +467,7 @@ def run_ours(args):
         dist.barrier()
     clocks = ClockSampler(device)
     clocks.start()
-    ms, launches, prof, _ = time_steps(sim, args.steps, args.warmup, seed, torch, profile=True)
+    ms, launches, _, _ = time_steps(sim, args.steps, args.warmup, seed, torch, profile=False)
     clk = clocks.stop()
     t = torch.tensor([ms], device="cuda")
     if dist:
@@ -475,6 +475,11 @@ def run_ours(args):
         dist.barrier()
     ms_max = float(t.item())
     value = ws * args.steps / (ms_max / 1e3)
+    # per-kernel breakdown from a separate pass with CUDA events around every
+    # launch (kept out of the timed region above)
+    sim.set_state(b0)
+    prof_steps = max(5, min(args.steps, 20))
+    ms_prof, _, prof, _ = time_steps(sim, prof_steps, 1, seed, torch, profile=True)
 
     # --- e2e through the C-ABI with host buffers ------------------------------
     e2e_value = None
@@ -491,12 +496,17 @@ def run_ours(args):
     # --- energy error mixed vs FP64 after --energy-steps steps ----------------
     rel_err = None
     fp64_value = None
+    fp64_e2e = None
     if args.energy_steps > 0 or args.fp64_steps > 0:
         sim64 = make_sim("fp64", device)
         sim64.set_state(b0)
         if args.fp64_steps > 0:
-            ms64, _, prof64, _ = time_steps(sim64, args.fp64_steps, 1, seed, torch, profile=True)
+            ms64, _, _, _ = time_steps(sim64, args.fp64_steps, 3, seed, torch, profile=False)
             fp64_value = args.fp64_steps / (ms64 / 1e3)
+            if not args.no_e2e and args.fp64_e2e_steps > 0:
+                sim64.set_state(b0)
+                e2e64_s, _, _ = time_e2e(sim64, args.fp64_e2e_steps, seed, torch)
+                fp64_e2e = args.fp64_e2e_steps / e2e64_s
         if args.energy_steps > 0:
             sim64.set_state(b0)
             sim64.step(args.energy_steps, seed)
@@ -530,6 +540,9 @@ def run_ours(args):
         step_bytes = 2 * sum(pbytes[k] for k in ("zinv_curl", "yinv", "xcross", "yfwd", "zfwd_epilogue"))
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
+                "timing": f"per-launch CUDA events on the library's stream over {prof_steps} steps, "
+                          f"a separate pass after the timed region ({ms_prof / prof_steps:.3f} ms/step "
+                          f"with the events, {ms_max / args.steps:.3f} without)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_s * 1e3,
                 "pruned": pruned,
@@ -546,13 +559,17 @@ def run_ours(args):
             "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps,
+            "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps, "warmup": 3,
+                     "e2e": {"value": fp64_e2e, "unit": UNIT, "steps": args.fp64_e2e_steps,
+                             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                      "bound": "fp64 alu (DADD/DFMA issue; HBM is not the limit)", "alu_probe_ginst_s": alu},
             "rel_energy_err_mixed_vs_fp64": rel_err, "energy_steps": args.energy_steps,
             "roofline": roof, "clocks": clk}
     sim.close()
     if rank == 0 and args.cufft_steps > 0:
         line["gpu_reference_style"] = cufft_baseline(b0, seed, device, args.cufft_steps, torch)
+    if rank == 0 and not args.no_extra:
+        line["other_configs"] = other_configs(torch)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -577,17 +594,17 @@ def _event_ms(fn, stream, torch):
     return e0.elapsed_time(e1)
 
 
-def run_precision(args):
+def measure_precision(n=256, nsteps=200):
     """256^3, 2D2C forcing, 200 steps: plain FP64 against mixed; steps/s of
     both and the mixed form's relative error in energy, helicity, viscous
     dissipation and the shell spectrum E(k), against the FP64 form (which
-    matches the FP64 oracle step by step, tests/test_gpu_golden.py)."""
+    matches the FP64 oracle step by step, tests/test_gpu_bench_path.py)."""
     import numpy as np
     import torch
     import gturbo3d_gb300 as g
     from gturbo3d_gb300.synth import initial_potential
     from gturbo3d_gb300.workloads import precision_params
-    n, nsteps, seed = args.size if args.size != 512 else 256, args.steps if args.steps != 50 else 200, 1
+    seed = 1
     b0 = initial_potential(n, n, n, seed)
     res = {}
     for prec in ("fp64", "mixed"):
@@ -603,13 +620,8 @@ def run_precision(args):
     ek64, ek32 = r64["spectrum"], r32["spectrum"]
     sig = ek64 > 1e-12 * ek64.max()
     rel = lambda a, b: abs(a - b) / abs(b) if b != 0 else None
-    line = {"metric": f"RK2 steps/s @{n}^3 2D2C, mixed vs FP64 diagnostics error after {nsteps} steps",
-            "value": r32["steps_per_s"], "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": 0,
-            "higher_is_better": True, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
-            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 1)",
-            "config": {"workload": f"rk2_step_{n}cubed_2d2c_precision", "grid": [n] * 3, "nu": 5e-4,
-                       "omega": 10.0, "dt": 2e-3, "forcing": "2d2c kz=0, 2<=|k_h|<=3, injection 0.1",
-                       "seed": seed},
+    return {"n": n, "steps": nsteps, "seed": seed,
+            "mixed": {"value": r32["steps_per_s"], "unit": UNIT},
             "fp64": {"value": r64["steps_per_s"], "unit": UNIT},
             "mixed_over_fp64": r32["steps_per_s"] / r64["steps_per_s"],
             "rel_err_mixed_vs_fp64": {"energy": rel(r32["energy"], r64["energy"]),
@@ -618,6 +630,21 @@ def run_precision(args):
                                       "spectrum_max_over_shells": float(np.max(np.abs(ek32[sig] - ek64[sig]) / ek64[sig])),
                                       "spectrum_shells_compared": int(sig.sum())},
             "values_fp64": {k: r64[k] for k in ("energy", "helicity", "dissipation")}}
+
+
+def run_precision(args):
+    n = args.size if args.size != 512 else 256
+    nsteps = args.steps if args.steps != 50 else 200
+    r = measure_precision(n, nsteps)
+    line = {"metric": f"RK2 steps/s @{n}^3 2D2C, mixed vs FP64 diagnostics error after {nsteps} steps",
+            "value": r["mixed"]["value"], "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": 0,
+            "higher_is_better": True, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
+            "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 1)",
+            "config": {"workload": f"rk2_step_{n}cubed_2d2c_precision", "grid": [n] * 3, "nu": 5e-4,
+                       "omega": 10.0, "dt": 2e-3, "forcing": "2d2c kz=0, 2<=|k_h|<=3, injection 0.1",
+                       "seed": r["seed"]},
+            "fp64": r["fp64"], "mixed_over_fp64": r["mixed_over_fp64"],
+            "rel_err_mixed_vs_fp64": r["rel_err_mixed_vs_fp64"], "values_fp64": r["values_fp64"]}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -681,7 +708,7 @@ def run_ensemble(args):
     return 0
 
 
-def run_adjoint(args):
+def measure_adjoint(n=128, nsteps=200):
     """128^3, 200 steps, forcing realisation of seed 3, J = kinetic energy of
     the shells |k| >= 20 after the run, gradient w.r.t. the initial vector
     potential with checkpoints every 20 steps.  FP64: TL/adjoint dot product
@@ -692,8 +719,6 @@ def run_adjoint(args):
     import gturbo3d_gb300 as g
     from gturbo3d_gb300.synth import initial_potential
     from gturbo3d_gb300.workloads import adjoint_params, random_direction, spectral_inner
-    n = args.size if args.size != 512 else 128
-    nsteps = args.steps if args.steps != 50 else 200
     seed, every, kmin, h = 3, 20, 20.0, 1e-6
     b0 = initial_potential(n, n, n, seed)
     res = {}
@@ -734,18 +759,54 @@ def run_adjoint(args):
     g64, g32 = grads["fp64"], grads["mixed"]
     num = sum(float(np.sum(np.abs(a - b) ** 2)) for a, b in zip(g32, g64))
     den = sum(float(np.sum(np.abs(b) ** 2)) for b in g64)
+    return {"n": n, "steps": nsteps, "seed": seed, "checkpoint_every": every, "kmin": kmin, "fd_h": h,
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "mixed_gradient_rel_l2_vs_fp64": math.sqrt(num / den),
+            "mixed_J_rel_vs_fp64": abs(res["mixed"]["J"] - res["fp64"]["J"]) / abs(res["fp64"]["J"])}
+
+
+def run_adjoint(args):
+    n = args.size if args.size != 512 else 128
+    nsteps = args.steps if args.steps != 50 else 200
+    r = measure_adjoint(n, nsteps)
     line = {"metric": f"adjoint gradient @{n}^3, {nsteps} steps: max rel. error vs central differences (FP64)",
-            "value": res["fp64"]["fd_rel_err_max"], "unit": "relative error", "n_gpus": 1, "steps": nsteps,
+            "value": r["fp64"]["fd_rel_err_max"], "unit": "relative error", "n_gpus": 1, "steps": nsteps,
             "warmup": 0, "higher_is_better": False, "dtype": "f64 (plain form); f32 mixed form reported beside",
             "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 3; directions seeds 600..607)",
             "config": {"workload": f"adjoint_{n}cubed", "grid": [n] * 3, "nu": 1e-3, "omega": 5.0, "dt": 4e-3,
                        "forcing": "3d3c realisation of seed 3", "objective": "kinetic energy of |k| >= 20",
-                       "checkpoint_every": every, "fd_h": h, "directions": 8},
-            "fp64": res["fp64"], "mixed": res["mixed"],
-            "mixed_gradient_rel_l2_vs_fp64": math.sqrt(num / den),
-            "mixed_J_rel_vs_fp64": abs(res["mixed"]["J"] - res["fp64"]["J"]) / abs(res["fp64"]["J"])}
+                       "checkpoint_every": r["checkpoint_every"], "fd_h": r["fd_h"], "directions": 8},
+            "fp64": r["fp64"], "mixed": r["mixed"],
+            "mixed_gradient_rel_l2_vs_fp64": r["mixed_gradient_rel_l2_vs_fp64"],
+            "mixed_J_rel_vs_fp64": r["mixed_J_rel_vs_fp64"]}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def other_configs(torch):
+    """Compact results of the 256^3 2D2C precision configuration and the
+    128^3 adjoint configuration, carried in the default line."""
+    out = {}
+    try:
+        r = measure_precision(256, 200)
+        out["precision_256cubed_2d2c_200_steps"] = {
+            "mixed_steps_per_s": r["mixed"]["value"], "fp64_steps_per_s": r["fp64"]["value"],
+            "mixed_over_fp64": r["mixed_over_fp64"], "rel_err_mixed_vs_fp64": r["rel_err_mixed_vs_fp64"]}
+    except Exception as ex:   # a reported result, not the headline measurement
+        out["precision_256cubed_2d2c_200_steps"] = {"error": str(ex)[:200]}
+    torch.cuda.empty_cache()
+    try:
+        r = measure_adjoint(128, 200)
+        f = r["fp64"]
+        out["adjoint_128cubed_200_steps"] = {
+            "fd_rel_err_max_fp64": f["fd_rel_err_max"], "fd_rel_err_fp64": f["fd_rel_err"],
+            "fd_target": 1e-6, "dot_product_rel_fp64": f["dot_product_rel"],
+            "mixed_gradient_rel_l2_vs_fp64": r["mixed_gradient_rel_l2_vs_fp64"],
+            "gradient_over_forward_fp64": f["gradient_over_forward"]}
+    except Exception as ex:
+        out["adjoint_128cubed_200_steps"] = {"error": str(ex)[:200]}
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -755,7 +816,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--energy-steps", type=int, default=100)
-    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--fp64-e2e-steps", type=int, default=10)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the compact 256^3 2D2C and 128^3 adjoint results of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cufft-steps", type=int, default=3,
                     help="timed steps of the reference-style cuFFT (torch.fft) GPU baseline; 0 skips it")

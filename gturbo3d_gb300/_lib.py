@@ -55,6 +55,8 @@ SIGNATURES = {
     "gt_params_validate": (C.c_int, [_P(GtParams)]),
     "gt_params_read": (C.c_int, [C.c_char_p, _P(GtParams)]),
     "gt_memory_estimate": (C.c_int, [_P(GtParams), _P(C.c_size_t)]),
+    "gt_set_memory_budget": (C.c_int, [C.c_uint64]),
+    "gt_get_memory_budget": (C.c_int, [_P(C.c_uint64)]),
     "gt_rann": (C.c_int, [_ip, C.c_int32, _P(C.c_float)]),
     "gt_forced_modes": (C.c_int, [_P(GtParams), _ip, _ip, _ip, _ip, _dp, _dp, _dp]),
     "gt_forcing_increments": (C.c_int, [_P(GtParams), _ip, C.c_int32, _ip, _ip, _ip, _ip, _dp]),
@@ -83,10 +85,10 @@ SIGNATURES = {
     "gt_check_finite": (C.c_int, [_vp]),
     "gt_set_pruning": (C.c_int, [_vp, C.c_int32]),
     "gt_pruning_active": (C.c_int, [_vp, _ip]),
-    "gt_set_pipelining": (C.c_int, [_vp, C.c_int32]),
     "gt_selftest_wait_timeout": (C.c_int, [_vp]),
     "gt_probe_alu": (C.c_int, [C.c_int32, _dp]),
     "gt_set_tuning": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
+    "gt_get_tuning": (C.c_int, [_vp, C.c_char_p, _ip]),
     "gt_autotune": (C.c_int, [_vp, C.c_char_p, _dp]),
     "gt_tl_step": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "gt_adj_step": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp]),

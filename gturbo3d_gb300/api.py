@@ -59,6 +59,25 @@ def read_params(path: str, base: GtParams | None = None) -> GtParams:
     return p
 
 
+def memory_estimate(p: GtParams) -> int:
+    """Device bytes gt_create allocates for p."""
+    n = C.c_size_t()
+    check(load().gt_memory_estimate(C.byref(p), C.byref(n)), "gt_memory_estimate")
+    return n.value
+
+
+def set_memory_budget(nbytes: int) -> None:
+    """Process-wide cap on one handle's device bytes (0 = none): gt_create
+    returns GT_ENOMEM above it, decided on the host before any CUDA call."""
+    check(load().gt_set_memory_budget(C.c_uint64(int(nbytes))), "gt_set_memory_budget")
+
+
+def memory_budget() -> int:
+    v = C.c_uint64()
+    check(load().gt_get_memory_budget(C.byref(v)), "gt_get_memory_budget")
+    return v.value
+
+
 def probe_alu(device: int = 0) -> dict:
     """This GPU's ALU issue rates (gt_probe_alu), G thread-instructions/s."""
     lib = load()
@@ -291,11 +310,13 @@ class Simulation:
         when the wait ran out as it should)."""
         return self.lib.gt_selftest_wait_timeout(self.h)
 
-    def set_pipelining(self, enable: bool) -> None:
-        check(self.lib.gt_set_pipelining(self.h, 1 if enable else 0), "gt_set_pipelining")
-
     def set_tuning(self, key: str, value: int) -> None:
         check(self.lib.gt_set_tuning(self.h, key.encode(), int(value)), f"gt_set_tuning({key})")
+
+    def get_tuning(self, key: str) -> int:
+        v = C.c_int32()
+        check(self.lib.gt_get_tuning(self.h, key.encode(), C.byref(v)), f"gt_get_tuning({key})")
+        return v.value
 
     def set_pruning(self, enable: bool) -> None:
         check(self.lib.gt_set_pruning(self.h, 1 if enable else 0), "gt_set_pruning")

@@ -150,14 +150,10 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
     return put(c.data(), c.size() * sizeof(R));
   };
   const size_t o_twx = puttw(g.nx), o_twy = puttw(g.ny), o_twz = puttw(g.nz);
-  std::vector<int32_t> tiles, tiles_p;
+  std::vector<int32_t> tiles;
   build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles);
   if (tiles.empty()) tiles = {0, 0};
   const size_t o_tiles = put(tiles.data(), tiles.size() * sizeof(int32_t));
-  const int ztx = zpipe_tx(g, (int)sizeof(Cplx<R>));
-  build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles_p, ztx > 0 ? ztx : 1);
-  if (tiles_p.empty()) tiles_p = {0, 0};
-  const size_t o_tiles_p = put(tiles_p.data(), tiles_p.size() * sizeof(int32_t));
   size_t o_tl[11];
   int n_tl[11];
   for (int lg = 0; lg < 11; ++lg) {
@@ -191,8 +187,6 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   t.truncate = h->p.truncate;
   t.ztiles = dptr<const int32_t>(mem, o_tiles);
   t.nztiles = (int)(tiles.size() / 2);
-  t.ztiles_p = dptr<const int32_t>(mem, o_tiles_p);
-  t.nztiles_p = (int)(tiles_p.size() / 2);
   for (int lg = 0; lg < 11; ++lg) {
     t.ztl[lg] = dptr<const int32_t>(mem, o_tl[lg]);
     t.nztl[lg] = n_tl[lg];
@@ -228,18 +222,9 @@ void free_handle(gt_handle* h) {
 }
 
 // ---- dispatch on precision ----------------------------------------------
-// The launch-shape state for one call: the tuning knobs always apply; the
-// TMA-pipelined variants only while pipelining is on and their tensor maps
-// exist.
-PipeMaps effective_tuning(const gt_handle* h) {
-  PipeMaps pm = h->pm;
-  if (!h->use_pipe || !pm.valid) pm.pipe_y = pm.pipe_z = pm.pipe_x = 0;
-  return pm;
-}
-
 int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
         int pruned) {
-  const PipeMaps pm = effective_tuning(h);
+  const PassTuning& pm = h->pm;
   if (h->mixed)
     return launch_nlt<float>(h->g, h->t32, a, bcor, out, h->w, mode, pruned, &pm, h->d_err, h->stream,
                              hook_fn, h);
@@ -249,7 +234,7 @@ int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3],
 
 // Both nonlinear terms of one RK2 step, b -> c -> b (main.f90:124-146).
 int rk2_nlts(gt_handle* h, int pruned) {
-  const PipeMaps pm = effective_tuning(h);
+  const PassTuning& pm = h->pm;
   if (h->mixed)
     return launch_rk2_nlts<float>(h->g, h->t32, h->b, h->c, h->w, pruned, &pm, h->d_err, h->stream,
                                   hook_fn, h);
@@ -440,10 +425,18 @@ int gt_create(const gt_params* p, gt_handle** out) {
   const int align = 128 / h->csize;
   g.nhp = (g.nh + align - 1) / align * align;
   g.lnx = ilog2(g.nx); g.lny = ilog2(g.ny); g.lnz = ilog2(g.nz);
-  cudaError_t e = cudaSetDevice(p->device);
-  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaSetDevice"); }
   size_t need = 0;
   gt_memory_estimate(p, &need);
+  uint64_t budget = 0;
+  gt_get_memory_budget(&budget);
+  if (budget > 0 && need > budget) {   // decided on the host, before any CUDA call
+    g_last_error = "grid needs " + std::to_string(need) + " device bytes, over the budget of " +
+                   std::to_string(budget) + " set by gt_set_memory_budget";
+    delete h;
+    return GT_ENOMEM;
+  }
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaSetDevice"); }
   size_t freeb = 0, totalb = 0;
   e = cudaMemGetInfo(&freeb, &totalb);
   if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaMemGetInfo"); }
@@ -484,7 +477,6 @@ int gt_create(const gt_params* p, gt_handle** out) {
   CKH(cudaMalloc(&h->d_count, sizeof(unsigned long long)));
   CKH(cudaMalloc(&h->d_err, sizeof(int)));
   CKH(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-  if (make_ypipe_maps(g, h->csize, h->w, h->pm) != 0) h->pm.valid = 0;
   // default x pass per grid: the parking variant where it measured faster
   // (FP32, NX = 512: 1.09 against 1.12 ms); at NX = 256 and 1024 and in FP64
   // the register-resident one
@@ -721,17 +713,25 @@ int gt_check_finite(gt_handle* h) {
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   if (!h || !key) return GT_EINVAL;
   const std::string k(key);
-  if (k == "pipe_y") h->pm.pipe_y = value != 0;
-  else if (k == "pipe_z") h->pm.pipe_z = value != 0;
-  else if (k == "pipe_x") h->pm.pipe_x = value != 0;
-  else if (k == "x_pairs" && value >= 1 && value <= 8) h->pm.x_pairs = value;
-  else if (k == "x_stages" && value >= 2 && value <= 4) h->pm.x_stages = value;
-  else if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
+  if (k == "y_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.y_tx = value;
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
   else if (k == "x_fused" && value >= 0 && value <= 3) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
+  else return GT_EINVAL;
+  return GT_OK;
+}
+
+int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
+  if (!h || !key || !value) return GT_EINVAL;
+  const std::string k(key);
+  if (k == "y_tx") *value = h->pm.y_tx;
+  else if (k == "z_tx") *value = h->pm.z_tx;
+  else if (k == "x_fused") *value = h->pm.x_fused;
+  else if (k == "y_pairs") *value = h->pm.y_pairs;
+  else if (k == "fuse_stage") *value = h->pm.fuse_stage;
+  else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;
   return GT_OK;
 }
@@ -742,12 +742,6 @@ int gt_selftest_wait_timeout(gt_handle* h) {
   if (rc) return rc;
   if ((rc = launch_wait_selftest(h->d_err, h->stream))) return cuda_fail((cudaError_t)rc, "launch_wait_selftest");
   return check_device_flag(h);
-}
-
-int gt_set_pipelining(gt_handle* h, int32_t enable) {
-  if (!h) return GT_EINVAL;
-  h->use_pipe = enable != 0;
-  return GT_OK;
 }
 
 int gt_set_pruning(gt_handle* h, int32_t enable) {

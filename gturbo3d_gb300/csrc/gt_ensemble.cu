@@ -117,6 +117,22 @@ extern "C" {
 int gt_ensemble_create(int32_t n, const gt_params* members, gt_ensemble** out) {
   if (n <= 0 || !members || !out) return GT_EINVAL;
   *out = nullptr;
+  // every member's parameters and memory budget are checked on the host
+  // before anything is allocated
+  uint64_t budget = 0;
+  gt_get_memory_budget(&budget);
+  for (int i = 0; i < n; ++i) {
+    if (members[i].device != members[0].device) return GT_EINVAL;
+    const int rc = gt_params_validate(&members[i]);
+    if (rc) return rc;
+    size_t need = 0;
+    gt_memory_estimate(&members[i], &need);
+    if (budget > 0 && need > budget) {
+      set_last_error("ensemble member " + std::to_string(i) + " needs " + std::to_string(need) +
+                     " device bytes, over the budget of " + std::to_string(budget));
+      return GT_ENOMEM;
+    }
+  }
   gt_ensemble* e = new (std::nothrow) gt_ensemble();
   if (!e) return GT_ENOMEM;
   e->device = members[0].device;

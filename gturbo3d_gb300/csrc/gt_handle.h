@@ -68,10 +68,8 @@ struct gt_handle {
   bool state_in_k = false;
   bool forcing_in_k = false;
   unsigned long long* d_count = nullptr;
-  // TMA-pipelined y passes (maps of the six work fields) and the device error
-  // flag their bounded waits raise
-  gt::PipeMaps pm{};
-  bool use_pipe = true;
+  // launch-shape knobs, and the device error flag that bounded device waits raise
+  gt::PassTuning pm{};
   int* d_err = nullptr;
   bool prof = false;
   std::vector<gtc::Pending> pending;
@@ -85,9 +83,6 @@ namespace gtc {
 // Launch hook of every kernel: counts launches and, when profiling, brackets
 // them with events.
 void hook_fn(void* ctx, int kind, bool begin);
-// The launch-shape state of one call (tuning knobs; pipelined variants only
-// while pipelining is on and their tensor maps exist).
-gt::PipeMaps effective_tuning(const gt_handle* h);
 // One nonlinear term in the handle's precision.
 int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3], int mode,
         int pruned = 0);
@@ -110,7 +105,7 @@ void free_handle(gt_handle* h);
 
 // Launch-shape knobs the autotuner searches.
 struct Tuning {
-  int pipe_y, pipe_z, pipe_x, x_pairs, x_stages, y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split;
+  int y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split;
 };
 
 Tuning get_tuning(const gt_handle* h);

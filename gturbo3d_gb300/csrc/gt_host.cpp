@@ -5,6 +5,7 @@
 // (inieuler.f90:14-20), seed and field files (main.f90:37-45, read.f90,
 // write.f90).  No CUDA here: everything in this file runs without a GPU.
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -337,10 +338,22 @@ static bool to_double(const std::string& s, double& v) {
   return end && *end == '\0' && end != s.c_str();
 }
 
+// A list-directed integer item: an optional sign and decimal digits only (a
+// Fortran integer read rejects "3.0" and "1e3"), within the int32 range.
 static bool to_int(const std::string& s, int32_t& v) {
-  double d;
-  if (!to_double(s, d) || d != std::floor(d)) return false;
-  v = (int32_t)d;
+  size_t i = 0;
+  bool neg = false;
+  if (i < s.size() && (s[i] == '+' || s[i] == '-')) neg = (s[i++] == '-');
+  if (i == s.size()) return false;
+  int64_t acc = 0;
+  for (; i < s.size(); ++i) {
+    if (s[i] < '0' || s[i] > '9') return false;
+    acc = acc * 10 + (s[i] - '0');
+    if (acc > (int64_t)INT32_MAX + 1) return false;   // stops before int64 overflow
+  }
+  if (neg) acc = -acc;
+  if (acc < (int64_t)INT32_MIN || acc > (int64_t)INT32_MAX) return false;
+  v = (int32_t)acc;
   return true;
 }
 
@@ -392,6 +405,21 @@ int gt_memory_estimate(const gt_params* p, size_t* bytes) {
   size_t total = 12 * field;
   total += (size_t)p->nz * p->ny * 4 + (size_t)(3 * 1024 + 1024 * 1024 * 3) * 8;
   *bytes = total;
+  return GT_OK;
+}
+
+namespace {
+std::atomic<uint64_t> g_memory_budget{0};
+}  // namespace
+
+int gt_set_memory_budget(uint64_t bytes) {
+  g_memory_budget.store(bytes);
+  return GT_OK;
+}
+
+int gt_get_memory_budget(uint64_t* bytes) {
+  if (!bytes) return GT_EINVAL;
+  *bytes = g_memory_budget.load();
   return GT_OK;
 }
 

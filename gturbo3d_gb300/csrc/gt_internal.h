@@ -8,7 +8,6 @@
 #include <string>
 #include <vector>
 
-#include <cuda.h>
 
 #include "../../include/gturbo_gb.h"
 
@@ -93,8 +92,6 @@ struct DevTables {
   // passes that contain such a column; xa = xcut[0] bounds every kept kx.
   const int32_t* ztiles;   // pairs (x-tile, y) for the default z tile width
   int nztiles;
-  const int32_t* ztiles_p; // the same for the tile width of the pipelined z pass
-  int nztiles_p;
   const int32_t* ztl[11];  // the same for every tile width 2^lg, lg = 0..10
   int nztl[11];
   int xa;
@@ -102,17 +99,10 @@ struct DevTables {
 
 enum NltMode { kNltOnly = 0, kStage1 = 1, kStage2 = 2 };
 
-// TMA tensor maps of the six work fields for the pipelined y passes
-// (box: 2*ytx scalars x 16 rows x 1 plane).
-struct PipeMaps {
-  CUtensorMap y[6];   // y passes: box 2*ytx x 16 rows x 1 plane, fields w[0..5]
-  CUtensorMap z[3];   // z forward pass: box 2*ztx x 1 row x min(nz,256) planes, w[0..2]
-  int ytx, ztx;
-  int valid;
-  // tuning: 0 = one-tile-per-CTA pass, 1 = pipelined (per pass)
-  int pipe_y = 0, pipe_z = 0, pipe_x = 0;
-  int x_pairs = 1, x_stages = 2;
-  int y_tx = 0, z_tx = 0;   // tile width of the plain y / z passes (0: default)
+// Launch-shape knobs of the passes (the gt_set_tuning keys); every setting
+// gives the same result up to rounding.
+struct PassTuning {
+  int y_tx = 0, z_tx = 0;   // tile width of the y / z passes (0: default)
   int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
   int x_fused = 2;          // x pass: 2 = one thread group per row pair, a row's three lines
                             // transformed together; 3 = the same with row 0's products
@@ -122,11 +112,6 @@ struct PipeMaps {
   int z_split = 0;          // z inverse pass: 1 = curl part and k^2 part in separate kernels;
                             // 2 = one one-region kernel, inputs read again per output line
 };
-using PFN_encodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                     const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                     const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                     CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-PFN_encodeTiled get_encode_tiled();
 
 // Work buffers: w[0..5] hold u_x,u_y,u_z,w_x,w_y,w_z between passes; after
 // the x-pass w[0..2] hold u x w.
@@ -149,28 +134,13 @@ const char* kernel_kind_name(int k);
 
 template <typename R>
 int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
-                    void* const w[6], int pruned, const PipeMaps* pm, int* err, void* stream,
+                    void* const w[6], int pruned, const PassTuning* pm, int* err, void* stream,
                     LaunchHook hook, void* hctx);
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+               void* const out[3], void* const w[6], int mode, int pruned, const PassTuning* pm,
                int* err, void* stream, LaunchHook hook, void* hctx);
-// Default tile width of the plain z passes (3 fields in shared memory).
-int ypipe_tx(const Geom& g, int csize);
-int zpipe_tx(const Geom& g, int csize);
 int launch_wait_selftest(int* err, void* stream);
-template <typename R>
-int launch_xpipe(const Geom& g, void* const w[6], const void* twx, int xa, int pairs, int nstage,
-                 int* err, void* stream, LaunchHook hook, void* hctx);
-template <typename R>
-int launch_zpipe_epi(const Geom& g, const DevTables<R>& tb, const PipeMaps& pm, void* const bcor[3],
-                     void* const out[3], int mode, int pruned, int* err, void* stream, LaunchHook hook,
-                     void* hctx);
-int make_ypipe_maps(const Geom& g, int csize, void* const w[6], PipeMaps& pm);
-template <typename R>
-int launch_ypipe(const Geom& g, const PipeMaps& pm, void* const* fields, int nf, const void* tw,
-                 int sign, int xlim, int ymask, const int32_t* xcut0, int* err, void* stream,
-                 LaunchHook hook, void* hctx);
 // (x-tile, y) blocks of the pruned z passes for precision with complex size csize.
 void build_ztiles(const Geom& g, const int32_t* xcut, int csize, std::vector<int32_t>& tiles,
                   int tx = 0);

@@ -1541,7 +1541,7 @@ template <typename R>
 // 2-4 (bit 1) and pass 5 (bit 2), so that the RK2 step can run the stage
 // boundary as one fused kernel in between.
 static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-                      void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+                      void* const out[3], void* const w[6], int mode, int pruned, const PassTuning* pm,
                       int* err, void* stream, LaunchHook hook, void* hctx, int phases) {
   int rc = set_smem_attrs<R>();
   if (rc) return rc;
@@ -1596,19 +1596,11 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   auto middle = [&](const Geom& gs, void* const* ws) -> int {
     int rc2 = 0;
     // pass 2
-    if (pm && pm->valid && pm->pipe_y) {
-      if ((rc2 = launch_ypipe<R>(gs, *pm, ws, 6, tb.twy, +1, xlim, pruned ? 1 : 0, tb.xcut, err, stream,
-                                 hook, hctx)))
-        return rc2;
-    } else if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut,
-                               ytx, ypairs))) {
+    if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
+                        ypairs)))
       return rc2;
-    }
     // pass 3
-    if (pm && pm->valid && pm->pipe_x) {
-      if ((rc2 = launch_xpipe<R>(gs, ws, tb.twx, xlim, pm->x_pairs, pm->x_stages, err, stream, hook, hctx)))
-        return rc2;
-    } else if (!pm || pm->x_fused) {
+    if (!pm || pm->x_fused) {
       // one group of nx/8 threads per row pair; as many groups per block as
       // fit in xfused_threads and divide the number of row pairs
       const int T = gs.nx / 8;
@@ -1654,23 +1646,11 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       if ((rc2 = (int)cudaGetLastError())) return rc2;
     }
     // pass 4
-    if (pm && pm->valid && pm->pipe_y) {
-      if ((rc2 = launch_ypipe<R>(gs, *pm, ws, 3, tb.twy, -1, xlim, pruned ? 2 : 0, tb.xcut, err, stream,
-                                 hook, hctx)))
-        return rc2;
-    } else if ((rc2 = spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut,
-                               ytx, ypairs))) {
-      return rc2;
-    }
-    return 0;
+    return spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs);
   };
   if ((phases & 2) && (rc = middle(g, w))) return rc;
   // pass 5
-  if (!(phases & 4)) {
-  } else if (pm && pm->valid && pm->pipe_z && pm->ztx > 0) {
-    if ((rc = launch_zpipe_epi<R>(g, tb, *pm, bcor, out, mode, pruned, err, stream, hook, hctx)))
-      return rc;
-  } else {
+  if (phases & 4) {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
     if (c.lgTX < zfwd_cols<R>() - 1) return (int)cudaErrorInvalidConfiguration;
     if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;
@@ -1695,7 +1675,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
 
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
-               void* const out[3], void* const w[6], int mode, int pruned, const PipeMaps* pm,
+               void* const out[3], void* const w[6], int mode, int pruned, const PassTuning* pm,
                int* err, void* stream, LaunchHook hook, void* hctx) {
   return nlt_phases<R>(g, tb, a, bcor, out, w, mode, pruned, pm, err, stream, hook, hctx, 7);
 }
@@ -1704,12 +1684,12 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
 // fuse_stage the first term's pass 5 and the second term's pass 1 run as the
 // fused k_zfwd_zinv (c stays on chip; four shared regions per tile, which
 // lowers occupancy: slower than the two passes at 512^3, 1.19 against 1.05 ms);
-// otherwise, and with the TMA-pipelined z pass, c goes through HBM.
+// otherwise c goes through HBM.
 template <typename R>
 int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
-                    void* const w[6], int pruned, const PipeMaps* pm, int* err, void* stream,
+                    void* const w[6], int pruned, const PassTuning* pm, int* err, void* stream,
                     LaunchHook hook, void* hctx) {
-  const bool fuse = pm && pm->fuse_stage && !(pm->valid && pm->pipe_z);
+  const bool fuse = pm && pm->fuse_stage;
   if (!fuse) {
     int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 7);
     if (rc) return rc;
@@ -1960,10 +1940,10 @@ const char* kernel_kind_name(int k) {
 
 #define GT_INST(R)                                                                              \
   template int launch_nlt<R>(const Geom&, const DevTables<R>&, void* const*, void* const*,     \
-                             void* const*, void* const*, int, int, const PipeMaps*, int*,      \
+                             void* const*, void* const*, int, int, const PassTuning*, int*,      \
                              void*, LaunchHook, void*);                                         \
   template int launch_rk2_nlts<R>(const Geom&, const DevTables<R>&, void* const*, void* const*, \
-                                  void* const*, int, const PipeMaps*, int*, void*, LaunchHook,  \
+                                  void* const*, int, const PassTuning*, int*, void*, LaunchHook,  \
                                   void*);                                                      \
   template int launch_count_outside<R>(const Geom&, const DevTables<R>&, void* const*,         \
                                        unsigned long long*, void*);                            \

@@ -22,6 +22,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "gt_internal.h"
 
 namespace {
@@ -31,11 +33,46 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxRows * 3];
 
-// Host-side device addresses of g_noalloc_scratch, one per device.  The
-// symbol's name in host code is only a stand-in; the address must come from
-// cudaGetSymbolAddress with the device current.
-double* g_scratch_addr[kMaxDevices] = {};
+// Host-side device addresses of g_noalloc_scratch, one per device, each
+// tagged with the id of the CUDA context it was looked up in.  The symbol's
+// name in host code is only a stand-in; the address must come from
+// cudaGetSymbolAddress with the device current.  A new primary context (after
+// cudaDeviceReset, or after the context was released and created again)
+// reloads the module and may place the array elsewhere, so a lookup is reused
+// only while the current context's id matches its tag.
+struct ScratchSlot {
+  double* addr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+ScratchSlot g_scratch_slot[kMaxDevices];
 std::mutex g_scratch_mu;
+
+using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
+using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context (driver entry points looked up
+// through the runtime, so the library need not link libcuda); false when it
+// cannot be read, in which case the address is looked up on every call.
+bool current_ctx_id(unsigned long long* id) {
+  static PFN_ctxGetCurrent get_current = nullptr;
+  static PFN_ctxGetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_ctxGetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_ctxGetId>(p);
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 void fail_msg(const char* msg) { gt::set_last_error(msg); }
 
@@ -44,7 +81,10 @@ int scratch_for_current_device(double** out) {
   if (cudaGetDevice(&dev) != cudaSuccess) return GT_ECUDA;
   if (dev < 0 || dev >= kMaxDevices) return GT_EINVAL;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  unsigned long long id = 0;
+  const bool have_id = current_ctx_id(&id);
+  ScratchSlot& slot = g_scratch_slot[dev];
+  if (!slot.addr || !have_id || slot.ctx_id != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -53,9 +93,10 @@ int scratch_for_current_device(double** out) {
       fail_msg(m);
       return GT_ECUDA;
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    slot.addr = static_cast<double*>(p);
+    slot.ctx_id = have_id ? id : 0;
   }
-  *out = g_scratch_addr[dev];
+  *out = slot.addr;
   return GT_OK;
 }
 

@@ -95,6 +95,14 @@ int gt_params_validate(const gt_params* p);
 int gt_params_read(const char* path, gt_params* p);
 /* Device bytes gt_create would allocate for p. */
 int gt_memory_estimate(const gt_params* p, size_t* bytes);
+/* Process-wide cap on the device bytes one handle may allocate (0 = no cap,
+ * the default).  gt_create (and every member of gt_ensemble_create) whose
+ * gt_memory_estimate exceeds it returns GT_ENOMEM before any CUDA call, so
+ * a driver that shares the GPU with other work can bound the library's
+ * footprint.  The reference has no counterpart: its arrays are static and
+ * an oversized grid fails at load or allocation time.  Host only. */
+int gt_set_memory_budget(uint64_t bytes);
+int gt_get_memory_budget(uint64_t* bytes);
 /* One draw of the reference's rann (forcing_3d3c.f90:82-93): advances
  * *irand and writes REAL*4(irand / (2^31-1)).  n draws in a row. */
 int gt_rann(int32_t* irand, int32_t n, float* out);
@@ -191,13 +199,8 @@ int gt_check_finite(gt_handle* h);
 int gt_set_pruning(gt_handle* h, int32_t enable);
 /* *active = 1 if the next gt_rk2_step takes the pruned path. */
 int gt_pruning_active(gt_handle* h, int32_t* active);
-/* TMA-pipelined y passes (on by default where the device supports them);
- * off selects the one-tile-per-CTA passes.  Results agree to rounding. */
-int gt_set_pipelining(gt_handle* h, int32_t enable);
 /* Launch-shape tuning (results are unchanged):
  * "y_tx", "z_tx" (0 = default, or 2/4/8/16: x-columns per block of the y / z passes),
- * "pipe_y", "pipe_z", "pipe_x" (0/1: TMA-pipelined persistent pass or one tile per block),
- * "x_pairs" (row pairs per pipelined x-pass block, 1..8), "x_stages" (2..4),
  * "x_fused" (x pass: 2 = one thread group per row pair, the three packed lines
  * of a row transformed together, u x w in registers (default); 3 = the same
  * with row 0's products parked in shared memory, three resident blocks per SM
@@ -210,6 +213,9 @@ int gt_set_pipelining(gt_handle* h, int32_t enable);
  * pass: 0 = one three-region kernel; 1 = w = k^2 a in its own one-region kernel;
  * 2 = one one-region kernel that reads the input columns again per output line). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
+/* The current value of one gt_set_tuning knob (the per-grid default until
+ * it is set). */
+int gt_get_tuning(gt_handle* h, const char* key, int32_t* value);
 
 /* Allocation-free kinetic energy, for callers that cannot allocate device
  * memory: a Fortran driver whose device arrays belong to another runtime (an
@@ -224,7 +230,10 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
  * every GPU that loads the library until the process exits; grids with
  * NY*NZ > 262144 rows are rejected with GT_EINVAL.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress, with
- * that device current), so make the first call before any stream capture.
+ * that device current), so make the first call before any stream capture;
+ * the lookup is kept per device and CUDA context and repeated after the
+ * context changes (after cudaDeviceReset the next call looks it up again and
+ * should likewise come before any capture).
  * All calls on a device share the array: calls that overlap on the GPU race
  * and must be serialised by the caller. */
 int gt_energy_noalloc(const double* bx, const double* by, const double* bz, int32_t nx,
@@ -282,7 +291,7 @@ int gt_ensemble_energy(gt_ensemble* e, double* energy);
 /* gt_autotune once per distinct (grid, precision) class, applied to all its members. */
 int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path);
 
-/* Exercises the bounded-wait failure path of the pipelined passes without a
+/* Exercises the bounded-wait failure path of the device waits without a
  * fault: a kernel waits on an mbarrier that nothing completes, gives up after a
  * few thousand polls and sets the handle's error flag.  Returns GT_ETIMEOUT
  * (and clears the flag); the handle stays usable.  No reference counterpart. */

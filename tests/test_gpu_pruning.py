@@ -51,28 +51,6 @@ def test_pruning_follows_the_state(lib):
         assert not sim.pruning_active                  # no truncation: nothing to prune
 
 
-@pytest.mark.parametrize("n", [(32, 32, 32), (64, 128, 16), (16, 16, 64), (32, 1024, 8)])
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-14), ("mixed", 2e-6)])
-@pytest.mark.parametrize("truncate", [1, 0])
-def test_pipelined_passes_equal_plain(lib, n, precision, tol, truncate):
-    """The TMA-pipelined persistent passes and narrower tiles give the result
-    of the default one-tile-per-block passes."""
-    import gturbo3d_gb300 as g
-    gp, _ = configs(n, precision=precision, forcing="3d3c", truncate=truncate)
-    gp.famp = g.forcing_amplitude(0.1, gp)
-    b0 = initial(n, seed=8)
-    with g.Simulation(gp) as a, g.Simulation(gp) as b:
-        a.set_state(b0)
-        b.set_state(b0)
-        for k in ("pipe_y", "pipe_z", "pipe_x"):
-            a.set_tuning(k, 1)
-        b.set_tuning("y_tx", 4)
-        b.set_tuning("z_tx", 4)
-        a.step(3, 17)
-        b.step(3, 17)
-        assert relerr(a.get_state(), b.get_state()) < tol
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,precision,tol", [(32, "fp64", 1e-13), (64, "mixed", 1e-5), (128, "mixed", 1e-5),
                                              ((8, 16, 16), "fp64", 1e-13), ((16, 32, 8), "mixed", 1e-5),

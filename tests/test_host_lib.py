@@ -238,3 +238,57 @@ def test_init_noise_large_grid_uses_jump_ahead(lib):
     ou, os_ = O.init_noise(O.Params(nx=128, ny=64, nz=64, dt=1e-3), 12345)
     assert s == os_
     assert all(np.array_equal(u[c], ou[c]) for c in range(3))
+
+
+def test_memory_budget_rejects_grid_on_host(lib):
+    """A grid whose device footprint is over the budget set with
+    gt_set_memory_budget gets GT_ENOMEM from gt_create, decided on the host
+    before any CUDA call (so this runs without a GPU), and leaves no handle;
+    the member check of gt_ensemble_create is the same one."""
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300 import _lib
+    p = g.make_params(512, precision="mixed")
+    need = g.memory_estimate(p)
+    assert g.memory_budget() == 0
+    try:
+        g.set_memory_budget(need - 1)
+        assert g.memory_budget() == need - 1
+        with pytest.raises(_lib.GturboError) as ei:
+            g.Simulation(p)
+        assert ei.value.code == _lib.GT_ENOMEM
+        assert "budget" in lib.gt_last_error().decode()
+        with pytest.raises(_lib.GturboError) as ei:
+            g.Ensemble([g.make_params(16), p])
+        assert ei.value.code == _lib.GT_ENOMEM
+    finally:
+        g.set_memory_budget(0)
+    assert g.memory_budget() == 0
+
+
+@pytest.mark.parametrize("text", ["3.0 1.5\n", "1e3 1.5\n", "99999999999 1.5\n", "-2147483649 1.5\n",
+                                  "inf 1.5\n", "nan 1.5\n", "+ 1.5\n"])
+def test_integer_items_are_strict(lib, tmp_path, text):
+    """Integer items (frame number, seed, npas, truncate) take an optional
+    sign and digits within the int32 range, as a Fortran integer read does;
+    anything else is GT_EIO rather than a silent conversion."""
+    import gturbo3d_gb300 as g
+    from gturbo3d_gb300 import _lib
+    f = tmp_path / "curframe.dat"
+    f.write_text(text)
+    with pytest.raises(_lib.GturboError) as ei:
+        g.read_frame(str(f))
+    assert ei.value.code == _lib.GT_EIO
+    f.write_text(text.split()[0] + "\n")
+    with pytest.raises(_lib.GturboError) as ei:
+        g.read_seed(str(f))
+    assert ei.value.code == _lib.GT_EIO
+
+
+def test_integer_item_limits(lib, tmp_path):
+    import gturbo3d_gb300 as g
+    f = tmp_path / "seed"
+    for v in (2147483647, -2147483648, 0, 7):
+        f.write_text(f"  {v}\n")
+        assert g.read_seed(str(f)) == v
+    f.write_text("+42\n")
+    assert g.read_seed(str(f)) == 42
