@@ -122,16 +122,21 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+GRID = None      # --grid NX NY NZ (profiling cases only; the default is N^3)
+
+
 def make_sim(precision, device, seed_offset=0):
     import gturbo3d_gb300 as g
-    p = g.make_params(N, precision=precision, forcing="3d3c", device=device, **PHYS)
+    nx, ny, nz = GRID if GRID else (N, N, N)
+    p = g.make_params(nx, ny, nz, precision=precision, forcing="3d3c", device=device, **PHYS)
     p.famp = g.forcing_amplitude(INJECTION, p)
     return g.Simulation(p)
 
 
 def initial_state(rank: int):
     from gturbo3d_gb300.synth import initial_potential
-    return initial_potential(N, N, N, SEED + rank)
+    nx, ny, nz = GRID if GRID else (N, N, N)
+    return initial_potential(nx, ny, nz, SEED + rank)
 
 
 def measured_peaks():
@@ -141,38 +146,40 @@ def measured_peaks():
         return None
 
 
-def pass_bytes(n, precision, pruned=True):
+def pass_bytes(n, precision, pruned=True, grid=None):
     """Algorithmic bytes per launch of each pass of one nonlinear term: every
     value a pass must read or write once (no padding, no re-reads).  With the
     2/3 truncation the pruned passes touch only the active (kx, ky) columns A,
-    the kept set K and kx < xa (the counts follow trunc.f90:14-17)."""
+    the kept set K and kx < xa (the counts follow trunc.f90:14-17).  grid =
+    (nx, ny, nz) for a non-cubic grid (2 pi box), else n^3."""
     import numpy as np
-    nh = n // 2 + 1
+    nx, ny, nz = grid if grid else (n, n, n)
+    nh = nx // 2 + 1
     esz = 8 if precision == "mixed" else 16
-    k = np.arange(n, dtype=float)
-    k = np.where(k > n // 2, k - n, k)
+
+    def freq(m):
+        k = np.arange(m, dtype=float)
+        return np.where(k > m // 2, k - m, k)
+
+    ky, kz = freq(ny), freq(nz)
     kx = np.arange(nh, dtype=float)
-    ks = (n // 2) ** 2
     rt = 0.6666666666666666667 ** 2
-    tz = (k * k) / ks
-    k1 = (tz[:, None, None] + ((k * k) / ks)[None, :, None]) + ((kx * kx) / ((n // 2) ** 2))[None, None, :]
+    k1 = ((kz * kz / (nz // 2) ** 2)[:, None, None] + (ky * ky / (ny // 2) ** 2)[None, :, None]) \
+        + (kx * kx / (nx // 2) ** 2)[None, None, :]
     over = k1 > rt
     xcut = np.where(over.any(axis=2), np.argmax(over, axis=2), nh)
-    if not pruned:
-        xcut[:] = nh
-    A = int(xcut[0].sum())
-    K = int(xcut.sum())
-    xa = int(xcut[0, 0])
-    rows = n * n
-    full = n * n * nh
-    if not pruned:
-        A, K, xa = n * nh, full, nh
+    rows = ny * nz
+    full = nz * ny * nh
+    if pruned:
+        A, K, xa = int(xcut[0].sum()), int(xcut.sum()), int(xcut[0, 0])
+    else:
+        A, K, xa = ny * nh, full, nh
     return {
-        "zinv_curl": (3 * K + 6 * A * n) * esz,
-        "yinv": (6 * A * n + 6 * xa * rows) * esz,
+        "zinv_curl": (3 * K + 6 * A * nz) * esz,
+        "yinv": (6 * A * nz + 6 * xa * rows) * esz,
         "xcross": (9 * xa * rows) * esz,
-        "yfwd": (3 * xa * rows + 3 * A * n) * esz,
-        "zfwd_epilogue": (3 * A * n + 6 * K) * esz,
+        "yfwd": (3 * xa * rows + 3 * A * nz) * esz,
+        "zfwd_epilogue": (3 * A * nz + 6 * K) * esz,
         "field_bytes": full * esz,
     }
 
@@ -527,7 +534,7 @@ def run_ours(args):
     # --- roofline of the dominant kernel --------------------------------------
     peaks = measured_peaks()
     hbm = peaks["hbm_gbs"] if peaks else 6800.0
-    pbytes = pass_bytes(N, "mixed", pruned=pruned)
+    pbytes = pass_bytes(N, "mixed", pruned=pruned, grid=GRID)
     passes = {k: v for k, v in prof.items() if k in pbytes} if prof else {}
     dom = max(passes.items(), key=lambda kv: kv[1][1]) if passes else None
     roof = None
@@ -536,7 +543,7 @@ def run_ours(args):
         per_launch_bytes = pbytes[name]
         avg_s = tms / nl / 1e3
         achieved = per_launch_bytes / avg_s / 1e9
-        traffic = ncu_traffic().get((name, "mixed")) if N == 512 else None
+        traffic = ncu_traffic().get((name, "mixed")) if (N == 512 and not GRID) else None
         step_bytes = 2 * sum(pbytes[k] for k in ("zinv_curl", "yinv", "xcross", "yfwd", "zfwd_epilogue"))
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
@@ -556,7 +563,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
             "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 2 + rank)",
-            "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+            "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                                       **({"grid": list(GRID), "profiling_grid": True} if GRID else {})}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps, "warmup": 3,
@@ -826,13 +834,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer timing (profiling runs)")
     ap.add_argument("--size", type=int, default=512,
                     help="grid size (512 default; 1024 runs the roofline sweep's second size with nu = 8e-5)")
+    ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="a non-cubic grid for profiling single kernels (the JSON line then describes it)")
     ap.add_argument("--workload", default="roofline", choices=["roofline", "precision", "ensemble", "adjoint"],
                     help="roofline: the headline 512^3 step (default); precision: 256^3 2D2C FP64 vs mixed; "
                          "ensemble: 64 uneven members, graph launch; adjoint: 128^3 gradient checks")
     args = ap.parse_args()
     global N
     global METRIC
+    global GRID
     N = args.size
+    GRID = tuple(args.grid) if args.grid else None
     METRIC = METRIC_FMT.format(n=N)
     if N >= 1024:
         PHYS["nu"] = 8e-5

@@ -432,6 +432,33 @@ __device__ __forceinline__ void fft_line_mem(E v[8], int t, const Cplx<R>* __res
   fft_stages_ct<SIGN, R, LGL, 0, PF>(v, t, tw, mem, sync, none);
 }
 
+// Asynchronous global -> shared copies (cp.async): B bytes (8 or 16) land at
+// sdst, of which the first src_bytes are read from gsrc and the rest are
+// zero-filled (src_bytes = 0 reads nothing).  Copies complete in commit
+// groups; a thread sees its own copies after cp_async_wait, other threads'
+// copies only after a barrier that follows their wait.
+template <int B>
+__device__ __forceinline__ void cp_async(void* sdst, const void* gsrc, int src_bytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  if constexpr (B == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(src_bytes)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(gsrc), "n"(B),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// Waits until at most n of this thread's commit groups are still in flight (n <= 3).
+__device__ __forceinline__ void cp_async_wait(int n) {
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+  }
+}
+
 // Strided shared-memory tile of a y or z pass: element e of column x of a
 // [rows][2^lg] tile, with one padding row after every 8 rows.  The padding
 // puts the rows that the threads of one 128-byte phase touch together in a

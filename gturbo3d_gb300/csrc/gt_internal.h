@@ -99,6 +99,21 @@ struct DevTables {
 
 enum NltMode { kNltOnly = 0, kStage1 = 1, kStage2 = 2 };
 
+// Members of one ensemble grid class advanced by the same launches: the
+// members' fields lie in one slab, member m's field f at member 0's field f
+// plus m * mstride elements; each member has its own integrating factor
+// (emk tables emk_len apart) and scalars (omega, dt, dt2 at scal[3 m]).  The
+// member index is a spare grid axis of every pass kernel.  nmem = 0: one
+// member, the launch of a single handle.
+template <typename R>
+struct Batch {
+  int nmem = 0;
+  long long mstride = 0;
+  const R* emk = nullptr;
+  int emk_len = 0;
+  const R* scal = nullptr;
+};
+
 // Launch-shape knobs of the passes (the gt_set_tuning keys); every setting
 // gives the same result up to rounding.
 struct PassTuning {
@@ -151,6 +166,12 @@ int launch_count_outside(const Geom& g, const DevTables<R>& tb, void* const b[3]
 template <typename R>
 int launch_force(const Geom& g, void* const b[3], const ForceEntry* entries, int n, int serial,
                  void* stream, LaunchHook hook, void* hctx);
+// Forcing of a grid class's members at step *step: member m adds its first
+// count[m] entries of base[(m * nsteps + *step) * nmax ...], then ++*step.
+template <typename R>
+int launch_force_batch(const Geom& g, void* const b[3], const Batch<R>& bt, const ForceEntry* base,
+                       const int* count, int nmax, int nsteps, const int* step, void* stream,
+                       LaunchHook hook, void* hctx);
 // Forcing of step *step from resident per-step entries, then ++*step.
 template <typename R>
 int launch_force_indexed(const Geom& g, void* const b[3], const ForceEntry* base, int n,

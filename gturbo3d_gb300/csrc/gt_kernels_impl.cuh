@@ -109,6 +109,17 @@ __device__ __forceinline__ void store_cols(Cplx<R>* __restrict__ p, size_t o, in
   }
 }
 
+// The same columns copied asynchronously into a shared-memory slot: the
+// slot receives what load_cols returns (columns >= lim zero-filled).
+template <typename R, int W>
+__device__ __forceinline__ void load_cols_async(ColT<R, W>* sdst, const Cplx<R>* __restrict__ p, size_t o,
+                                                int X0, int lim) {
+  constexpr int B = (int)sizeof(ColT<R, W>);
+  constexpr int CB = (int)sizeof(Cplx<R>);
+  const int n = X0 + W <= lim ? B : (X0 < lim ? (lim - X0) * CB : 0);
+  cp_async<B>(sdst, p + o, n);
+}
+
 // Columns per thread of the z inverse pass: 2 for FP32, 1 for FP64.  The z
 // forward pass keeps one column per thread: its epilogue works column by
 // column, and pairs measured slower there (0.49 ms against 0.46 ms at 512^3).
@@ -175,8 +186,23 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
     S1[idx(z)] = uy;
     S2[idx(z)] = uz;
   }
+  // The k^2 part re-reads a_c; its columns are copied asynchronously into
+  // region c as soon as the u_c transform has finished with that region (its
+  // last reads precede the transform's final barrier), so the copies run
+  // behind the remaining u transforms instead of stalling the k^2 ones.
+  auto prefetch = [&](int c3, E* S) {
+    const C* ac = reinterpret_cast<const C*>(a.at(c3));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+      load_cols_async<R, W>(S + idx(z), ac, (size_t)z * plane + base, X0, lim);
+    }
+    cp_async_commit();
+  };
   C* out0 = reinterpret_cast<C*>(w.p[0]);
   fft_line_ct<+1, R, LGZ>(v, t, tw, S0, idx);
+  if (k2part) prefetch(0, S0);
 #pragma unroll
   for (int i = 0; i < 8; ++i) store_cols<R, W>(out0, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   for (int f = 1; f < 3; ++f) {
@@ -185,18 +211,19 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
     for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
     __syncthreads();
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    if (k2part) prefetch(f, S);
     C* out = reinterpret_cast<C*>(w.at(f));
 #pragma unroll
     for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
   }
   if (!k2part) return;   // w = k^2 a by k_zk2 (no barrier follows)
   for (int c3 = 0; c3 < 3; ++c3) {
-    const C* ac = reinterpret_cast<const C*>(a.at(c3));
+    E* S = c3 == 0 ? S0 : (c3 == 1 ? S1 : S2);
+    cp_async_wait(2 - c3);   // this thread's copies of a_c3 have landed
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int z = t + i * T;
-      const int lim = valid ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
-      E av = load_cols<R, W>(ac, (size_t)z * plane + base, X0, lim);
+      E av = S[idx(z)];
       const R kzs = tb.fkzs[z];
 #pragma unroll
       for (int c = 0; c < W; ++c) {
@@ -206,7 +233,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
       }
       v[i] = av;
     }
-    E* S = c3 == 0 ? S0 : (c3 == 1 ? S1 : S2);
+    __syncthreads();   // every thread holds its inputs before the exchanges overwrite the region
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
     C* out = reinterpret_cast<C*>(w.at(3 + c3));
 #pragma unroll
@@ -786,11 +813,23 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   E v[8];
+  // all three fields' columns are copied asynchronously into their regions
+  // at once (one commit group per field), so the loads of fields 1 and 2 run
+  // behind the transform of field 0
   for (int f = 0; f < 3; ++f) {
     const C* in = reinterpret_cast<const C*>(w.at(f));
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = load_cols<R, W>(in, (size_t)(t + i * T) * plane + base, X0, ylim);
     E* S = sm + f * reg;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      load_cols_async<R, W>(S + idx(t + i * T), in, (size_t)(t + i * T) * plane + base, X0, ylim);
+    cp_async_commit();
+  }
+  for (int f = 0; f < 3; ++f) {
+    E* S = sm + f * reg;
+    cp_async_wait(2 - f);   // this thread's copies of field f have landed
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+    __syncthreads();        // every thread holds its inputs before the exchanges overwrite the region
     fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
 #pragma unroll
     for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
@@ -848,18 +887,18 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
         const R e = X >= g.nh ? (R)0
                     : (tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X]);
         C s0, s1, s2;
-        if (mode == kStage1) {  // rkstep.f90:126-135: c = emk (a + dt2 c)
+        if (mode == kStage1) {  // rkstep.f90:30-40: c = emk (a + dt2 c)
           const R d = tb.dt2;
           s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
           s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
           s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};
-        } else {                // rkstep.f90:182-191: a = emk (emk a + dt c)
+        } else {                // rkstep.f90:86-96: a = emk (emk a + dt c)
           const R d = tb.dt;
           s0 = C{e * (e * b0.x + d * r0.x), e * (e * b0.y + d * r0.y)};
           s1 = C{e * (e * b1.x + d * r1.x), e * (e * b1.y + d * r1.y)};
           s2 = C{e * (e * b2.x + d * r2.x), e * (e * b2.y + d * r2.y)};
         }
-        if (zero_mode) {        // rkstep.f90:140-144 / 196-200
+        if (zero_mode) {        // rkstep.f90:44-48 / 100-104
           s0 = C{0, 0}; s1 = C{0, 0}; s2 = C{0, 0};
         }
         col(res0, c) = s0; col(res1, c) = s1; col(res2, c) = s2;
@@ -874,7 +913,7 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 // ---------------------------------------------------------------------------
 // Passes 5 and 1 of the RK2 step fused at the stage boundary: the forward z
 // transform of the first nonlinear term and its stage-1 epilogue give
-// c = emk (b + dt2 N1) (rkstep.f90:126-144), which stays in shared memory
+// c = emk (b + dt2 N1) (rkstep.f90:30-48), which stays in shared memory
 // (regions 0-2, written in place of the transformed N1 at each thread's own
 // positions); the inverse z transforms of u = curl c and w = k^2 c for the
 // second nonlinear term (nlt.f90:26-40, produ.f90:44-63) follow, with region
@@ -945,7 +984,7 @@ k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, cons
       const int X = X0 + c;
       const bool zero_mode = (X == 0) && (y == 0) && (z == 0);
       C s0{0, 0}, s1{0, 0}, s2{0, 0};
-      if (X < wlim && !zero_mode) {           // rkstep.f90:140-144: c(0) = 0
+      if (X < wlim && !zero_mode) {           // rkstep.f90:44-48: c(0) = 0
         const C b0 = col(bb0, c), b1 = col(bb1, c), b2 = col(bb2, c);
         const C m0 = col(n0, c), m1 = col(n1, c), m2 = col(n2, c);
         const C a0{m0.x - okz * b0.y, m0.y + okz * b0.x};
@@ -961,7 +1000,7 @@ k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, cons
           r0 = C{0, 0}; r1 = C{0, 0}; r2 = C{0, 0};
         }
         const R e = tb.emk_by_k2 ? tb.emk[(int)k2] : tb.emk[((size_t)z * g.ny + y) * g.nh + X];
-        const R d = tb.dt2;                    // rkstep.f90:126-135
+        const R d = tb.dt2;                    // rkstep.f90:30-40
         s0 = C{e * (b0.x + d * r0.x), e * (b0.y + d * r0.y)};
         s1 = C{e * (b1.x + d * r1.x), e * (b1.y + d * r1.y)};
         s2 = C{e * (b2.x + d * r2.x), e * (b2.y + d * r2.y)};

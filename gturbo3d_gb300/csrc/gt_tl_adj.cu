@@ -21,8 +21,8 @@ using namespace gtc;
 //   adjoint (inner products of gt_adjoint.cu): with mu = invcurl P lam and
 //   g = fft_inv(mu):  lam_a = curl fft_dir(w x g) + k^2 fft_dir(g x u),
 //   lam_bc = -i omega kz mu.
-// The RK2 step and its zeroing of the k = 0 mode (rkstep.f90:140-144,
-// 196-200) are differentiated on top.
+// The RK2 step and its zeroing of the k = 0 mode (rkstep.f90:44-48,
+// 100-104) are differentiated on top.
 // ===========================================================================
 namespace {
 
