@@ -101,6 +101,8 @@ SIGNATURES = {
     "gt_ensemble_step": (C.c_int, [_vp, C.c_int32, _ip, C.c_int32]),
     "gt_ensemble_energy": (C.c_int, [_vp, _dp]),
     "gt_ensemble_autotune": (C.c_int, [_vp, C.c_char_p]),
+    "gt_ensemble_set_batching": (C.c_int, [_vp, C.c_int32]),
+    "gt_ensemble_info": (C.c_int, [_vp, _ip, _ip]),
     "gt_strerror": (C.c_char_p, [C.c_int]),
     "gt_last_error": (C.c_char_p, []),
     "gt_get_stream": (C.c_int, [_vp, _P(_vp)]),

@@ -424,8 +424,9 @@ def autotune(sim: "Simulation", cache_path: str | None = None) -> float:
 
 
 class Ensemble:
-    """Independent members advanced together (gt_ensemble_*): in graph mode one
-    captured CUDA graph launch advances every member by 64 steps."""
+    """Independent members advanced together (gt_ensemble_*): members of one
+    grid class share one launch per pass; in graph mode one captured CUDA
+    graph launch advances every member by 64 steps."""
 
     def __init__(self, params: list):
         self.lib = load()
@@ -481,3 +482,15 @@ class Ensemble:
     def autotune(self, cache_path: str | None = None):
         check(self.lib.gt_ensemble_autotune(self.h, cache_path.encode() if cache_path else None),
               "gt_ensemble_autotune")
+
+    def set_batching(self, enable: bool) -> None:
+        """One launch per pass for each grid class (on, the default) or per member."""
+        check(self.lib.gt_ensemble_set_batching(self.h, 1 if enable else 0), "gt_ensemble_set_batching")
+
+    def classes(self) -> list:
+        """Each member's grid class (-1: runs alone)."""
+        n = C.c_int32()
+        cls = np.zeros(self.n, np.int32)
+        check(self.lib.gt_ensemble_info(self.h, C.byref(n), cls.ctypes.data_as(C.POINTER(C.c_int32))),
+              "gt_ensemble_info")
+        return [int(x) for x in cls]

@@ -209,7 +209,7 @@ void free_handle(gt_handle* h) {
     if (h->h_force[i]) cudaFreeHost(h->h_force[i]);
     if (h->force_copied[i]) cudaEventDestroy(h->force_copied[i]);
   }
-  if (h->fields_mem) cudaFree(h->fields_mem);
+  if (h->fields_mem && h->owns_fields) cudaFree(h->fields_mem);
   if (h->stage) cudaFree(h->stage);
   if (h->tab_mem) cudaFree(h->tab_mem);
   if (h->d_partials) cudaFree(h->d_partials);
@@ -405,9 +405,9 @@ int set_dev(gt_handle* h) {
 
 }  // namespace gtc
 
-extern "C" {
-
-int gt_create(const gt_params* p, gt_handle** out) {
+// A handle; with ext_fields its twelve fields live in memory the caller
+// owns (an ensemble class slab) and are not freed with the handle.
+int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   if (!p || !out) return GT_EINVAL;
   *out = nullptr;
   int rc = gt_params_validate(p);
@@ -456,7 +456,12 @@ int gt_create(const gt_params* p, gt_handle** out) {
   } while (0)
   CKH(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   const size_t fbytes = g.field_elems() * h->csize;
-  CKH(cudaMalloc(&h->fields_mem, 12 * fbytes));
+  if (ext_fields) {
+    h->fields_mem = ext_fields;
+    h->owns_fields = false;
+  } else {
+    CKH(cudaMalloc(&h->fields_mem, 12 * fbytes));
+  }
   CKH(cudaMemsetAsync(h->fields_mem, 0, 12 * fbytes, h->stream));
   for (int c = 0; c < 3; ++c) {
     h->b[c] = dptr<void>(h->fields_mem, c * fbytes);
@@ -492,6 +497,10 @@ int gt_create(const gt_params* p, gt_handle** out) {
   *out = h;
   return GT_OK;
 }
+
+extern "C" {
+
+int gt_create(const gt_params* p, gt_handle** out) { return create_handle(p, out, nullptr); }
 
 int gt_destroy(gt_handle* h) {
   if (!h) return GT_EINVAL;
@@ -717,6 +726,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
   else if (k == "x_fused" && value >= 0 && value <= 3) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
+  else if (k == "y_prefetch") h->pm.y_prefetch = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
   else return GT_EINVAL;
@@ -730,6 +740,7 @@ int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
   else if (k == "z_tx") *value = h->pm.z_tx;
   else if (k == "x_fused") *value = h->pm.x_fused;
   else if (k == "y_pairs") *value = h->pm.y_pairs;
+  else if (k == "y_prefetch") *value = h->pm.y_prefetch;
   else if (k == "fuse_stage") *value = h->pm.fuse_stage;
   else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;

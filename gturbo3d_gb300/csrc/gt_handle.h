@@ -43,6 +43,7 @@ struct gt_handle {
   int csize = 16;
   cudaStream_t stream = nullptr;
   void* fields_mem = nullptr;
+  bool owns_fields = true;     // false: the fields live in an ensemble class slab
   void* b[3]{};
   void* c[3]{};
   void* w[6]{};
@@ -102,10 +103,12 @@ int run_steps(gt_handle* h, int nsteps, const std::vector<gt::ForceEntry>& all,
 // Makes the handle's device current and clears a stale non-sticky error.
 int set_dev(gt_handle* h);
 void free_handle(gt_handle* h);
+// gt_create, with the twelve fields optionally in caller-owned device memory.
+int create_handle(const gt_params* p, gt_handle** out, void* ext_fields);
 
 // Launch-shape knobs the autotuner searches.
 struct Tuning {
-  int y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split;
+  int y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split, y_prefetch;
 };
 
 Tuning get_tuning(const gt_handle* h);

@@ -119,6 +119,8 @@ struct Batch {
 struct PassTuning {
   int y_tx = 0, z_tx = 0;   // tile width of the y / z passes (0: default)
   int y_pairs = 1;          // FP32 y passes: 1 = two adjacent columns per thread
+  int y_prefetch = 0;       // FP32 y passes (with y_pairs): 1 = persistent blocks that double-buffer
+                            // their tiles with asynchronous copies
   int x_fused = 2;          // x pass: 2 = one thread group per row pair, a row's three lines
                             // transformed together; 3 = the same with row 0's products
                             // parked in shared memory (the default for FP32 at NX = 512);
@@ -150,7 +152,7 @@ const char* kernel_kind_name(int k);
 template <typename R>
 int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
                     void* const w[6], int pruned, const PassTuning* pm, int* err, void* stream,
-                    LaunchHook hook, void* hctx);
+                    LaunchHook hook, void* hctx, const Batch<R>* bt = nullptr);
 template <typename R>
 int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
                void* const out[3], void* const w[6], int mode, int pruned, const PassTuning* pm,

@@ -48,6 +48,21 @@ struct Ptr6 {
   }
 };
 
+// Element offset of member m's fields in a batched launch (0 for one member).
+__device__ __forceinline__ size_t member_offset(long long mstride, unsigned m) {
+  return mstride ? (size_t)m * (size_t)mstride : 0;
+}
+
+// A batched launch's member m: its own integrating factor and scalars.
+template <typename R>
+__device__ __forceinline__ void member_tables(const Batch<R>& bt, unsigned m, DevTables<R>& tb) {
+  if (!bt.nmem) return;
+  tb.emk = bt.emk + (size_t)m * bt.emk_len;
+  tb.omega = bt.scal[3 * m];
+  tb.dt = bt.scal[3 * m + 1];
+  tb.dt2 = bt.scal[3 * m + 2];
+}
+
 constexpr int kSmemBudget = 200 * 1024;
 
 template <typename R> constexpr int max_threads() { return sizeof(R) == 8 ? 512 : 1024; }
@@ -129,7 +144,7 @@ template <typename R> constexpr int zfwd_cols() { return 1; }
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>() / zcols<R>())
 k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
-            int k2part) {
+            int k2part, long long mstride) {
   using C = Cplx<R>;
   constexpr int W = zcols<R>();
   using E = ColT<R, W>;
@@ -147,7 +162,7 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
   const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(mstride, pruned ? blockIdx.y : blockIdx.z);
   const int reg = strided_rows(1 << LGZ) * TP;
   E* S0 = sm;
   E* S1 = sm + reg;
@@ -250,7 +265,8 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 // ---------------------------------------------------------------------------
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(kSpassThreads, sizeof(R) == 8 ? 2 : 3)
-k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
+      long long mstride) {
   using C = Cplx<R>;
   constexpr int W = zcols<R>();
   using E = ColT<R, W>;
@@ -258,10 +274,13 @@ k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32
   E* sm = reinterpret_cast<E*>(smraw);
   const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
   const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
-  int tile = blockIdx.x, y = blockIdx.z;
+  // grid: (tiles, field, member) pruned; (tiles, field, member * ny + y) full
+  int tile = blockIdx.x, y = blockIdx.z % g.ny;
+  unsigned mem = blockIdx.z / g.ny;
   if (pruned) {
     tile = tiles[2 * blockIdx.x];
     y = tiles[2 * blockIdx.x + 1];
+    mem = blockIdx.z;
   }
   const int f = blockIdx.y;
   const int X0 = tile * TX + W * xp;
@@ -269,7 +288,7 @@ k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32
   const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(mstride, mem);
   const StridedIdxLg idx{lgTP, xp};
   R kxs[W];
 #pragma unroll
@@ -308,7 +327,8 @@ k_zk2(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32
 // ---------------------------------------------------------------------------
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(kSpassThreads, sizeof(R) == 8 ? 2 : 3)
-k_zinv_curl1(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+k_zinv_curl1(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
+             long long mstride) {
   using C = Cplx<R>;
   constexpr int W = zcols<R>();
   using E = ColT<R, W>;
@@ -326,7 +346,7 @@ k_zinv_curl1(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, cons
   const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(mstride, pruned ? blockIdx.y : blockIdx.z);
   const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
   R kx[W], kxs[W];
@@ -396,7 +416,7 @@ template <typename R> constexpr int spass_min_blocks() { return sizeof(R) == 8 ?
 template <typename R, int SIGN, int LGL>
 __global__ void __launch_bounds__(kSpassThreads, spass_min_blocks<R>())
 k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, int xlim,
-        int ymask, const int32_t* __restrict__ xcut0) {
+        int ymask, const int32_t* __restrict__ xcut0, int nf, long long mstride) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -405,8 +425,9 @@ k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, i
   const int X = blockIdx.x * TX + x;
   const bool valid = X < xlim;
   constexpr int T = 1 << (LGL - 3);
-  C* p = reinterpret_cast<C*>(f.at(blockIdx.z));
-  const size_t base = (size_t)blockIdx.y * (size_t)os + (valid ? X : 0);
+  // blockIdx.z = member * nf + field
+  C* p = reinterpret_cast<C*>(f.at(blockIdx.z % nf));
+  const size_t base = (size_t)blockIdx.y * (size_t)os + (valid ? X : 0) + member_offset(mstride, blockIdx.z / nf);
   const StridedIdxLg idx{lgTX, x};
   C v[8];
   // ymask 1 (pruned inverse y pass): only (X, y) with X < xcut0[y] hold data;
@@ -441,7 +462,7 @@ k_spass(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTX, i
 template <int SIGN, int LGL>
 __global__ void __launch_bounds__(kSpassThreads, SIGN > 0 ? 4 : 3)
 k_spass2(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTP, int xlim, int ymask,
-         const int32_t* __restrict__ xcut0) {
+         const int32_t* __restrict__ xcut0, int nf, long long mstride) {
   using C = float2;
   using E = CPair<float>;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -450,8 +471,9 @@ k_spass2(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTP, 
   const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
   const int X0 = 2 * (blockIdx.x * TP + xp);
   constexpr int T = 1 << (LGL - 3);
-  C* p = reinterpret_cast<C*>(f.at(blockIdx.z));
-  const size_t base = (size_t)blockIdx.y * (size_t)os + (X0 < xlim ? X0 : 0);
+  // blockIdx.z = member * nf + field
+  C* p = reinterpret_cast<C*>(f.at(blockIdx.z % nf));
+  const size_t base = (size_t)blockIdx.y * (size_t)os + (X0 < xlim ? X0 : 0) + member_offset(mstride, blockIdx.z / nf);
   const StridedIdxLg idx{lgTP, xp};
   E v[8];
 #pragma unroll
@@ -478,6 +500,88 @@ k_spass2(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTP, 
       dst[0] = v[i].a;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 strided transform as a persistent pass: each block walks tiles
+// (x-tile fastest, then the outer index, field and member) and double-buffers
+// them in shared memory; the next tile's columns are copied asynchronously
+// (cp.async, zero-filled where the truncation masks them) while the current
+// tile is transformed, so every block keeps a tile of loads in flight instead
+// of stalling on them between transforms.  Same columns, masks and results as
+// k_spass2.
+// ---------------------------------------------------------------------------
+template <int SIGN, int LGL>
+__global__ void __launch_bounds__(kSpassThreads, 3)
+k_spass2_pf(Ptr6 f, Geom g, const void* twv, long long ls, long long os, int lgTP, int xlim, int ymask,
+            const int32_t* __restrict__ xcut0, int nf, long long mstride, int ntx, int nouter,
+            long long nitems) {
+  using C = float2;
+  using E = CPair<float>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  constexpr int T = 1 << (LGL - 3);
+  const int stage_elems = strided_rows(1 << LGL) * TP;
+  E* const st0 = reinterpret_cast<E*>(smraw);
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(twv);
+  // item -> (field pointer, element base, first column)
+  auto locate = [&](long long item, C*& p, size_t& base, int& X0) {
+    const int tx = (int)(item % ntx);
+    const long long r = item / ntx;
+    const int outer = (int)(r % nouter);
+    const int fz = (int)(r / nouter);   // member * nf + field
+    X0 = 2 * (tx * TP + xp);
+    p = reinterpret_cast<C*>(f.at(fz % nf));
+    base = (size_t)outer * (size_t)os + (X0 < xlim ? X0 : 0) + member_offset(mstride, fz / nf);
+  };
+  auto prefetch = [&](long long item, E* S) {
+    C* p;
+    size_t base;
+    int X0;
+    locate(item, p, base, X0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = t + i * T;
+      const int cut = ymask == 1 ? min(xlim, xcut0[e]) : xlim;
+      const int n = X0 + 1 < cut ? 16 : (X0 < cut ? 8 : 0);
+      cp_async<16>(S + idx(e), p + base + (size_t)e * (size_t)ls, n);
+    }
+  };
+  long long item = blockIdx.x;
+  if (item < nitems) prefetch(item, st0);
+  cp_async_commit();
+  for (int it = 0; item < nitems; item += gridDim.x, ++it) {
+    E* S = st0 + (it & 1) * stage_elems;
+    // the other stage was last used by the previous tile, whose final
+    // barrier every thread has passed
+    if (item + gridDim.x < nitems) prefetch(item + gridDim.x, st0 + ((it + 1) & 1) * stage_elems);
+    cp_async_commit();
+    cp_async_wait(1);   // this thread's copies of the current tile have landed
+    E v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+    __syncthreads();    // every thread holds its inputs before the exchanges overwrite the stage
+    fft_line_ct<SIGN, float, LGL>(v, t, tw, S, idx);
+    C* p;
+    size_t base;
+    int X0;
+    locate(item, p, base, X0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = t + i * T;
+      const int cut = ymask == 2 ? min(xlim, xcut0[e]) : xlim;
+      C* dst = p + base + (size_t)e * (size_t)ls;
+      if (X0 + 1 < cut) {
+        *reinterpret_cast<E*>(dst) = v[i];
+      } else if (X0 < cut) {
+        dst[0] = v[i].a;
+      }
+    }
+    if constexpr (LGL == 3) __syncthreads();   // no barrier in a one-stage transform: free the stage
+  }
+  cp_async_wait(0);   // nothing in flight at exit
 }
 
 // ---------------------------------------------------------------------------
@@ -517,7 +621,7 @@ __device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R
 
 template <typename R, int LGN>
 __global__ void __launch_bounds__(xcross_threads<LGN>(), (xcross_min_blocks<R, LGN>()))
-k_xcross(Ptr6 w, Geom g, const void* twv, int P, R shalf, int xa) {
+k_xcross(Ptr6 w, Geom g, const void* twv, int P, R shalf, int xa, long long mstride) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -528,13 +632,14 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, R shalf, int xa) {
   const size_t pair = (size_t)blockIdx.x * P + p;
   const C* tw = reinterpret_cast<const C*>(twv);
   const size_t nhp = g.nhp;
+  const size_t mo = member_offset(mstride, blockIdx.y);   // batched launch: member blockIdx.y
   C v[8];
   // inverse: rows 0 and 1 of the pair, field pair q
 #pragma unroll 1
   for (int r = 0; r < 2; ++r) {
     const size_t row = 2 * pair + r;
-    const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + row * nhp;
-    const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + row * nhp;
+    const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + mo + row * nhp;
+    const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + mo + row * nhp;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
     const SwzIdx idx{(p * 6 + r * 3 + q) * LP};
@@ -581,7 +686,7 @@ k_xcross(Ptr6 w, Geom g, const void* twv, int P, R shalf, int xa) {
     for (int r = 0; r < 2; ++r) {
       const int o = (r == 0 ? lineA : lineB) * LP;
       const bool first = (q == 0) || (q == 2 && r == 0);
-      C* orow = out + (2 * pair + r) * nhp;
+      C* orow = out + mo + (2 * pair + r) * nhp;
       for (int k = t; k < xa; k += T) {
         const int kb = (N - k) & (N - 1);
         const C a = sm[o + swz(k)], b = sm[o + swz(kb)];
@@ -606,7 +711,7 @@ template <typename R> constexpr int xfused_threads() { return sizeof(R) == 8 ? 1
 
 template <typename R, int LGN>
 __global__ void __launch_bounds__(xfused_threads<R>(), 2)
-k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
+k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
   using C = Cplx<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
@@ -617,6 +722,7 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
   const size_t pair = (size_t)blockIdx.x * P + grp;
   const C* tw = reinterpret_cast<const C*>(twv);
   const size_t nhp = g.nhp;
+  const size_t mo = member_offset(mstride, blockIdx.y);   // batched launch: member blockIdx.y
   const SwzIdx idx{grp * LP};
   C* line = sm + grp * LP;
   C v[8], z0[8], z1[8];
@@ -627,8 +733,8 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
       const size_t row = 2 * pair + r;
 #pragma unroll 1
       for (int q = 0; q < 3; ++q) {
-        const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + row * nhp;
-        const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + row * nhp;
+        const C* X1 = reinterpret_cast<const C*>(w.at(2 * q)) + mo + row * nhp;
+        const C* X2 = reinterpret_cast<const C*>(w.at(2 * q + 1)) + mo + row * nhp;
 #pragma unroll
         for (int i = 0; i < 8; ++i) v[i] = pack_c2r<R>(X1, X2, t + i * T, N, xa);
         fft_line_ct<+1, R, LGN>(v, t, tw, sm, idx, sync);
@@ -665,8 +771,8 @@ k_xfused(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
         for (int i = 0; i < 8; ++i) sm[idx(t + i * T)] = v[i];
         sync();
         // pass 0: Z = c_x + i c_y of row r; pass 1: Z = c_z(row 0) + i c_z(row 1)
-        C* oa = reinterpret_cast<C*>(pass == 0 ? w.p[0] : w.p[2]) + (pass == 0 ? row : 2 * pair) * nhp;
-        C* ob = reinterpret_cast<C*>(pass == 0 ? w.p[1] : w.p[2]) + (pass == 0 ? row : 2 * pair + 1) * nhp;
+        C* oa = reinterpret_cast<C*>(pass == 0 ? w.p[0] : w.p[2]) + mo + (pass == 0 ? row : 2 * pair) * nhp;
+        C* ob = reinterpret_cast<C*>(pass == 0 ? w.p[1] : w.p[2]) + mo + (pass == 0 ? row : 2 * pair + 1) * nhp;
         for (int k = t; k < xa; k += T) {
           const int kb = (N - k) & (N - 1);
           const C a = line[swz(k)], b = line[swz(kb)];
@@ -699,7 +805,7 @@ template <typename R> constexpr int xbatch_threads() { return sizeof(R) == 8 ? 1
 // group) instead of registers, for 3 resident blocks instead of 2.
 template <typename R, int LGN, bool PARK = false>
 __global__ void __launch_bounds__(xbatch_threads<R>(), PARK ? 3 : 2)
-k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
+k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
   using C = Cplx<R>;
   using E = CTrip<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -710,6 +816,7 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
   const size_t pair = (size_t)blockIdx.x * P + grp;
   const C* tw = reinterpret_cast<const C*>(twv);
   const size_t nhp = g.nhp;
+  const size_t mo = member_offset(mstride, blockIdx.y);   // batched launch: member blockIdx.y
   C* lines = sm + (size_t)grp * 3 * LP;
   const TripMem<R, SwzIdx> mem{lines, SwzIdx{0}, LP};
   E v[8];
@@ -724,12 +831,12 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int e = t + i * T;
-        v[i].a = pack_c2r<R>(reinterpret_cast<const C*>(w.p[0]) + row * nhp,
-                             reinterpret_cast<const C*>(w.p[1]) + row * nhp, e, N, xa);
-        v[i].b = pack_c2r<R>(reinterpret_cast<const C*>(w.p[2]) + row * nhp,
-                             reinterpret_cast<const C*>(w.p[3]) + row * nhp, e, N, xa);
-        v[i].c = pack_c2r<R>(reinterpret_cast<const C*>(w.p[4]) + row * nhp,
-                             reinterpret_cast<const C*>(w.p[5]) + row * nhp, e, N, xa);
+        v[i].a = pack_c2r<R>(reinterpret_cast<const C*>(w.p[0]) + mo + row * nhp,
+                             reinterpret_cast<const C*>(w.p[1]) + mo + row * nhp, e, N, xa);
+        v[i].b = pack_c2r<R>(reinterpret_cast<const C*>(w.p[2]) + mo + row * nhp,
+                             reinterpret_cast<const C*>(w.p[3]) + mo + row * nhp, e, N, xa);
+        v[i].c = pack_c2r<R>(reinterpret_cast<const C*>(w.p[4]) + mo + row * nhp,
+                             reinterpret_cast<const C*>(w.p[5]) + mo + row * nhp, e, N, xa);
       }
       fft_line_mem<+1, R, LGN, (sizeof(R) == 4 && !PARK)>(v, t, tw, mem, sync);
       // u = (z0.x, z0.y, z1.x), w = (z1.y, z2.x, z2.y) (produ.f90:14-16)
@@ -770,8 +877,8 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 #pragma unroll
       for (int pl = 0; pl < 3; ++pl) {
         const C a = lines[pl * LP + ia], b = lines[pl * LP + ib];
-        C* oa = (pl == 2 ? f2 : f0) + (row0 + (pl == 1 ? 1 : 0)) * nhp;
-        C* ob = (pl == 2 ? f2 : f1) + (row0 + (pl == 0 ? 0 : 1)) * nhp;
+        C* oa = (pl == 2 ? f2 : f0) + mo + (row0 + (pl == 1 ? 1 : 0)) * nhp;
+        C* ob = (pl == 2 ? f2 : f1) + mo + (row0 + (pl == 0 ? 0 : 1)) * nhp;
         oa[k] = split_r2c<R>(a, b, true, shalf);
         ob[k] = split_r2c<R>(a, b, false, shalf);
       }
@@ -790,7 +897,7 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa) {
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>() / zfwd_cols<R>())
 k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
-           const int32_t* __restrict__ tiles) {
+           const int32_t* __restrict__ tiles, Batch<R> bt) {
   using C = Cplx<R>;
   constexpr int W = zfwd_cols<R>();
   using E = ColT<R, W>;
@@ -808,7 +915,9 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const unsigned mem = pruned ? blockIdx.y : blockIdx.z;
+  member_tables(bt, mem, tb);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(bt.mstride, mem);
   const int reg = strided_rows(1 << LGZ) * TP;
   const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
@@ -922,7 +1031,8 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
 // ---------------------------------------------------------------------------
 template <typename R, int LGZ>
 __global__ void __launch_bounds__(max_threads<R>() / 2 / zcols<R>())
-k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles) {
+k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
+            Batch<R> bt) {
   using C = Cplx<R>;
   constexpr int W = zcols<R>();
   using E = ColT<R, W>;
@@ -940,7 +1050,9 @@ k_zfwd_zinv(Ptr6 w, Ptr6 bc, DevTables<R> tb, Geom g, int lgTX, int pruned, cons
   const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
   const size_t plane = (size_t)g.ny * g.nhp;
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const unsigned mem = pruned ? blockIdx.y : blockIdx.z;
+  member_tables(bt, mem, tb);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(bt.mstride, mem);
   const int reg = strided_rows(1 << LGZ) * TP;
   const StridedIdxLg idx{lgTP, xp};
   const C* tw = reinterpret_cast<const C*>(tb.twz);
@@ -1216,6 +1328,29 @@ __global__ void k_force_indexed(Ptr6 b, const ForceEntry* __restrict__ base, int
   }
 }
 
+// Forcing of the members of a batched launch (blockIdx.y = member): member m
+// adds its first count[m] entries of step *step; entries [m][nsteps][nmax].
+template <typename R>
+__global__ void k_force_batch(Ptr6 b, const ForceEntry* __restrict__ base, const int* __restrict__ count,
+                              int nmax, int nsteps, const int* __restrict__ step, Geom g, long long mstride) {
+  using C = Cplx<R>;
+  const unsigned mem = blockIdx.y;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count[mem]) return;
+  const ForceEntry en = base[((size_t)mem * nsteps + *step) * nmax + e];
+  const size_t o = ((size_t)en.z * g.ny + en.y) * g.nhp + en.x + member_offset(mstride, mem);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (!(en.mask & (1 << c))) continue;
+    C* p = reinterpret_cast<C*>(b.at(c));
+    const C v = p[o];
+    if (sizeof(R) == 8)
+      p[o] = C{(R)((double)v.x + en.inc[2 * c]), (R)((double)v.y + en.inc[2 * c + 1])};
+    else
+      p[o] = C{v.x + (R)en.inc[2 * c], v.y + (R)en.inc[2 * c + 1]};
+  }
+}
+
 static __global__ void k_step_inc(int* step) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
 }
@@ -1479,7 +1614,7 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 14 + 1];
+  cudaError_t es[8 * 16 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
@@ -1490,6 +1625,8 @@ static int set_smem_attrs() {
   if (sizeof(R) == 4) {                                  \
     es[n++] = allow_smem(k_spass2<1, LG>, optin);        \
     es[n++] = allow_smem(k_spass2<-1, LG>, optin);       \
+    es[n++] = allow_smem(k_spass2_pf<1, LG>, optin);     \
+    es[n++] = allow_smem(k_spass2_pf<-1, LG>, optin);    \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
@@ -1527,7 +1664,8 @@ static int set_smem_attrs() {
 template <typename R>
 static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int axis, int sign,
                  cudaStream_t s, LaunchHook hook, void* hctx, int xlim = -1, int ymask = 0,
-                 const int32_t* xcut0 = nullptr, int force_tx = 0, bool pairs = false) {
+                 const int32_t* xcut0 = nullptr, int force_tx = 0, bool pairs = false, int nmem = 1,
+                 long long mstride = 0, int prefetch = 0) {
   const int csize = sizeof(Cplx<R>);
   const int L = axis == 1 ? g.ny : g.nz;
   const int lgL = axis == 1 ? g.lny : g.lnz;
@@ -1549,26 +1687,52 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
     if (c2.lgTX >= 1) {
       const int TX2 = 1 << c2.lgTX;
       const int ntx2 = (xlim + TX2 - 1) / TX2;
-      dim3 grid2(ntx2, outer, nf);
+      if (prefetch) {
+        // persistent, double-buffered: three blocks per SM
+        static int nsm = 0;
+        if (!nsm) {
+          int dev = 0;
+          cudaGetDevice(&dev);
+          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+          if (nsm <= 0) nsm = 1;
+        }
+        const long long nitems = (long long)ntx2 * outer * nf * nmem;
+        const unsigned blocks = (unsigned)std::min<long long>(nitems, 3LL * nsm);
+        GT_HOOK(kind, true);
+#define GT_L(LG)                                                                                      \
+  if (sign > 0)                                                                                       \
+    k_spass2_pf<1, LG><<<blocks, c2.threads / 2, 2 * c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, \
+                                                                   xcut0, nf, mstride, ntx2, outer, nitems); \
+  else                                                                                                \
+    k_spass2_pf<-1, LG><<<blocks, c2.threads / 2, 2 * c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim,  \
+                                                                    ymask, xcut0, nf, mstride, ntx2, outer, nitems);
+        GT_DISPATCH_LG(lgL, GT_L)
+#undef GT_L
+        GT_HOOK(kind, false);
+        return (int)cudaGetLastError();
+      }
+      dim3 grid2(ntx2, outer, nf * nmem);
       GT_HOOK(kind, true);
 #define GT_L(LG)                                                                                      \
   if (sign > 0)                                                                                       \
-    k_spass2<1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0); \
+    k_spass2<1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0, \
+                                                            nf, mstride);                                  \
   else                                                                                                \
-    k_spass2<-1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0);
+    k_spass2<-1, LG><<<grid2, c2.threads / 2, c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0, \
+                                                             nf, mstride);
       GT_DISPATCH_LG(lgL, GT_L)
 #undef GT_L
       GT_HOOK(kind, false);
       return (int)cudaGetLastError();
     }
   }
-  dim3 grid(ntx, outer, nf);
+  dim3 grid(ntx, outer, nf * nmem);
   GT_HOOK(kind, true);
 #define GT_L(LG)                                                                                  \
   if (sign > 0)                                                                                   \
-    k_spass<R, 1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0); \
+    k_spass<R, 1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0, nf, mstride); \
   else                                                                                            \
-    k_spass<R, -1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0);
+    k_spass<R, -1, LG><<<grid, c.threads, c.smem, s>>>(f, g, tw, ls, os, c.lgTX, xlim, ymask, xcut0, nf, mstride);
   GT_DISPATCH_LG(lgL, GT_L)
 #undef GT_L
   GT_HOOK(kind, false);
@@ -1581,9 +1745,14 @@ template <typename R>
 // boundary as one fused kernel in between.
 static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], void* const bcor[3],
                       void* const out[3], void* const w[6], int mode, int pruned, const PassTuning* pm,
-                      int* err, void* stream, LaunchHook hook, void* hctx, int phases) {
+                      int* err, void* stream, LaunchHook hook, void* hctx, int phases,
+                      const Batch<R>* bt = nullptr) {
   int rc = set_smem_attrs<R>();
   if (rc) return rc;
+  // a batched launch covers nm members (a spare grid axis), their fields mstride apart
+  const Batch<R> bb = bt ? *bt : Batch<R>{};
+  const unsigned nm = bb.nmem > 0 ? (unsigned)bb.nmem : 1u;
+  const long long mstride = bb.nmem > 0 ? bb.mstride : 0;
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
   const int ztx = pm ? pm->z_tx : 0;
@@ -1595,7 +1764,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     Ptr6 pa{}, pw{};
     for (int i = 0; i < 3; ++i) pa.p[i] = a[i];
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
-    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
+    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX], nm) : dim3(c.ntiles, g.ny, nm);
     GT_HOOK(kKZinvCurl, true);
     const bool fits = c.threads / zcols<R>() <= kSpassThreads;
     const int split = pm && pm->z_split == 1 && fits ? 1 : 0;
@@ -1603,21 +1772,22 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       // one shared region, the input columns read again per output line
 #define GT_L(LG)                                                                                   \
   k_zinv_curl1<R, LG><<<grid, c.threads / zcols<R>(), c.smem / 3, s>>>(pa, pw, tb, g, c.lgTX, pruned, \
-                                                                       tb.ztl[c.lgTX]);
+                                                                       tb.ztl[c.lgTX], mstride);
       GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     } else {
 #define GT_L(LG)                                                                                   \
   k_zinv_curl<R, LG><<<grid, c.threads / zcols<R>(), c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned,    \
-                                                                  tb.ztl[c.lgTX], split ? 0 : 1);
+                                                                  tb.ztl[c.lgTX], split ? 0 : 1, mstride);
       GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     }
     if (split && !(rc = (int)cudaGetLastError())) {
       // w = k^2 a: one field per block, one shared region (a third of the smem)
-      const dim3 grid2 = pruned ? dim3(tb.nztl[c.lgTX], 3) : dim3(c.ntiles, 3, g.ny);
+      const dim3 grid2 = pruned ? dim3(tb.nztl[c.lgTX], 3, nm) : dim3(c.ntiles, 3, g.ny * nm);
       const int smem1 = c.smem / 3;
-#define GT_L(LG) k_zk2<R, LG><<<grid2, c.threads / zcols<R>(), smem1, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX]);
+#define GT_L(LG) \
+  k_zk2<R, LG><<<grid2, c.threads / zcols<R>(), smem1, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX], mstride);
       GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     }
@@ -1635,8 +1805,9 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   auto middle = [&](const Geom& gs, void* const* ws) -> int {
     int rc2 = 0;
     // pass 2
+    const int ypf = pm ? pm->y_prefetch : 0;
     if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
-                        ypairs)))
+                        ypairs, (int)nm, mstride, ypf)))
       return rc2;
     // pass 3
     if (!pm || pm->x_fused) {
@@ -1652,18 +1823,20 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
       GT_HOOK(kKXCross, true);
       if (!pm || pm->x_fused == 2) {
-#define GT_L(LG) k_xbatch<R, LG><<<(unsigned)(npairs / P), P * T, 3 * smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+#define GT_L(LG) \
+  k_xbatch<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, 3 * smem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       } else if (pm->x_fused == 3) {
         // three planes and the parking region (N complex + N real per group)
         const int psmem = 3 * smem + smem + smem / 2;
 #define GT_L(LG) \
-  k_xbatch<R, LG, true><<<(unsigned)(npairs / P), P * T, psmem, s>>>(pw, gs, tb.twx, shalf, xlim);
+  k_xbatch<R, LG, true><<<dim3((unsigned)(npairs / P), nm), P * T, psmem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       } else {
-#define GT_L(LG) k_xfused<R, LG><<<(unsigned)(npairs / P), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim);
+#define GT_L(LG) \
+  k_xfused<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       }
@@ -1678,14 +1851,16 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       Ptr6 pw{};
       for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
       GT_HOOK(kKXCross, true);
-#define GT_L(LG) k_xcross<R, LG><<<(unsigned)nblocks, threads, smem, s>>>(pw, gs, tb.twx, P, shalf, xlim);
+#define GT_L(LG) \
+  k_xcross<R, LG><<<dim3((unsigned)nblocks, nm), threads, smem, s>>>(pw, gs, tb.twx, P, shalf, xlim, mstride);
       GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       GT_HOOK(kKXCross, false);
       if ((rc2 = (int)cudaGetLastError())) return rc2;
     }
     // pass 4
-    return spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs);
+    return spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs,
+                    (int)nm, mstride, ypf);
   };
   if ((phases & 2) && (rc = middle(g, w))) return rc;
   // pass 5
@@ -1699,11 +1874,11 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       pb.p[i] = bcor[i];
       po.p[i] = out[i];
     }
-    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX]) : dim3(c.ntiles, g.ny);
+    const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX], nm) : dim3(c.ntiles, g.ny, nm);
     GT_HOOK(kKZFwdEpi, true);
 #define GT_L(LG)                                                                                   \
   k_zfwd_epi<R, LG><<<grid, c.threads / zfwd_cols<R>(), c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, \
-                                                                 pruned, tb.ztl[c.lgTX]);
+                                                                 pruned, tb.ztl[c.lgTX], bb);
     GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     GT_HOOK(kKZFwdEpi, false);
@@ -1727,14 +1902,16 @@ int launch_nlt(const Geom& g, const DevTables<R>& tb, void* const a[3], void* co
 template <typename R>
 int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], void* const c[3],
                     void* const w[6], int pruned, const PassTuning* pm, int* err, void* stream,
-                    LaunchHook hook, void* hctx) {
+                    LaunchHook hook, void* hctx, const Batch<R>* bt) {
   const bool fuse = pm && pm->fuse_stage;
   if (!fuse) {
-    int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 7);
+    int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 7, bt);
     if (rc) return rc;
-    return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 7);
+    return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 7, bt);
   }
-  int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 1 | 2);
+  const Batch<R> bb = bt ? *bt : Batch<R>{};
+  const unsigned nm = bb.nmem > 0 ? (unsigned)bb.nmem : 1u;
+  int rc = nlt_phases<R>(g, tb, b, b, c, w, kStage1, pruned, pm, err, stream, hook, hctx, 1 | 2, bt);
   if (rc) return rc;
   {
     const int csize = sizeof(Cplx<R>);
@@ -1746,17 +1923,17 @@ int launch_rk2_nlts(const Geom& g, const DevTables<R>& tb, void* const b[3], voi
     Ptr6 pw{}, pb{};
     for (int i = 0; i < 6; ++i) pw.p[i] = w[i];
     for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
-    const dim3 grid = pruned ? dim3(tb.nztl[cf.lgTX]) : dim3(cf.ntiles, g.ny);
+    const dim3 grid = pruned ? dim3(tb.nztl[cf.lgTX], nm) : dim3(cf.ntiles, g.ny, nm);
     GT_HOOK(kKZFwdZinv, true);
 #define GT_L(LG)                                                                                  \
   k_zfwd_zinv<R, LG><<<grid, cf.threads / zcols<R>(), cf.smem, s>>>(pw, pb, tb, g, cf.lgTX, pruned, \
-                                                                   tb.ztl[cf.lgTX]);
+                                                                   tb.ztl[cf.lgTX], bb);
     GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     GT_HOOK(kKZFwdZinv, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }
-  return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 2 | 4);
+  return nlt_phases<R>(g, tb, c, b, b, w, kStage2, pruned, pm, err, stream, hook, hctx, 2 | 4, bt);
 }
 
 template <typename R>
@@ -1781,6 +1958,21 @@ int launch_force_indexed(const Geom& g, void* const b[3], const ForceEntry* base
   GT_HOOK(kKForce, true);
   if (n > 0)
     k_force_indexed<R><<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(pb, base, n, step, g);
+  k_step_inc<<<1, 32, 0, (cudaStream_t)stream>>>(const_cast<int*>(step));
+  GT_HOOK(kKForce, false);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+int launch_force_batch(const Geom& g, void* const b[3], const Batch<R>& bt, const ForceEntry* base,
+                       const int* count, int nmax, int nsteps, const int* step, void* stream,
+                       LaunchHook hook, void* hctx) {
+  Ptr6 pb{};
+  for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  GT_HOOK(kKForce, true);
+  if (nmax > 0 && bt.nmem > 0)
+    k_force_batch<R><<<dim3((nmax + 127) / 128, bt.nmem), 128, 0, (cudaStream_t)stream>>>(
+        pb, base, count, nmax, nsteps, step, g, bt.mstride);
   k_step_inc<<<1, 32, 0, (cudaStream_t)stream>>>(const_cast<int*>(step));
   GT_HOOK(kKForce, false);
   return (int)cudaGetLastError();
@@ -1983,13 +2175,16 @@ const char* kernel_kind_name(int k) {
                              void*, LaunchHook, void*);                                         \
   template int launch_rk2_nlts<R>(const Geom&, const DevTables<R>&, void* const*, void* const*, \
                                   void* const*, int, const PassTuning*, int*, void*, LaunchHook,  \
-                                  void*);                                                      \
+                                  void*, const Batch<R>*);                                     \
   template int launch_count_outside<R>(const Geom&, const DevTables<R>&, void* const*,         \
                                        unsigned long long*, void*);                            \
   template int launch_force<R>(const Geom&, void* const*, const ForceEntry*, int, int, void*,  \
                                LaunchHook, void*);                                              \
   template int launch_force_indexed<R>(const Geom&, void* const*, const ForceEntry*, int,      \
                                        const int*, void*, LaunchHook, void*);                  \
+  template int launch_force_batch<R>(const Geom&, void* const*, const Batch<R>&,                \
+                                     const ForceEntry*, const int*, int, int, const int*, void*, \
+                                     LaunchHook, void*);                                        \
   template int launch_convert<R>(const Geom&, const void*, void*, int, void*, LaunchHook,      \
                                  void*);                                                        \
   template int launch_fft_inv<R>(const Geom&, const DevTables<R>&, void*, void*, void* const*, \

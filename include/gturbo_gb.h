@@ -282,14 +282,24 @@ int gt_ensemble_get_state(gt_ensemble* e, int32_t member, double* bx, double* by
 /* nsteps RK2 steps of every member; seeds[n] are the members' forcing seeds
  * (advanced).  The forcing is drawn on the host in chunks of 64 steps.
  * graph = 1: one captured CUDA graph launch per chunk advances every member
- * by 64 steps (each member's kernels on its own stream, joined at the end of
- * the chunk; a shorter last chunk is launched directly); graph = 0: the same
- * kernels launched member by member and step by step. */
+ * by 64 steps (each class's batched launches, or a lone member's kernels, on
+ * their own stream, joined at the end of the chunk; a shorter last chunk is
+ * launched directly); graph = 0: the same launches issued directly. */
 int gt_ensemble_step(gt_ensemble* e, int32_t nsteps, int32_t* seeds, int32_t graph);
 /* Total kinetic energy of each member (n values). */
 int gt_ensemble_energy(gt_ensemble* e, double* energy);
 /* gt_autotune once per distinct (grid, precision) class, applied to all its members. */
 int gt_ensemble_autotune(gt_ensemble* e, const char* cache_path);
+/* Batched launches (on by default): members of one grid class (same grid, box,
+ * precision and truncation; two or more members) keep their fields in one
+ * device slab and every pass of the step runs as one launch for the whole
+ * class, each member with its own integrating factor, Omega, dt and forcing;
+ * classes and lone members run concurrently.  Off: each member's kernels are
+ * launched on their own.  Results are the same either way. */
+int gt_ensemble_set_batching(gt_ensemble* e, int32_t enable);
+/* *nclasses = number of grid classes; class_of[i] (n values, may be NULL) =
+ * member i's class, or -1 for a member that runs alone. */
+int gt_ensemble_info(gt_ensemble* e, int32_t* nclasses, int32_t* class_of);
 
 /* Exercises the bounded-wait failure path of the device waits without a
  * fault: a kernel waits on an mbarrier that nothing completes, gives up after a

@@ -82,3 +82,83 @@ def test_autotune_and_cache(lib, tmp_path):
         assert relerr(tuned.get_state(), plain.get_state()) < 1e-6
     text = open(cache).read()
     assert '"key": "64x64x64/mixed/pruned/' in text
+
+
+def _class_members():
+    """Three grid classes of two or more members (different Omega, nu, dt,
+    forcing kind and forcing count within a class) and two lone members."""
+    import gturbo3d_gb300 as g
+    specs = [((32, 32, 32), "mixed", "3d3c", 3.0, 1e-3, 2e-3), ((32, 32, 32), "mixed", "3d3c", 11.0, 2e-3, 3e-3),
+             ((32, 32, 32), "mixed", "2d2c", 17.0, 5e-4, 1e-3), ((32, 16, 8), "fp64", "3d3c", 2.0, 1e-3, 2e-3),
+             ((32, 16, 8), "fp64", "none", 9.0, 3e-3, 4e-3), ((16, 16, 16), "fp64", "3d3c", 5.0, 1e-3, 2e-3),
+             ((64, 32, 16), "mixed", "3d3c", 4.0, 1e-3, 2e-3), ((16, 16, 16), "mixed", "3d3c", 6.0, 1e-3, 2e-3),
+             ((16, 16, 16), "mixed", "3d3c", 7.0, 2e-3, 1e-3)]
+    params, states = [], []
+    for k, (n, prec, forcing, om, nu, dt) in enumerate(specs):
+        gp, _ = configs(n, precision=prec, forcing=forcing, omega=om, nu=nu, dt=dt)
+        if forcing != "none":
+            gp.famp = g.forcing_amplitude(0.1, gp)
+        params.append(gp)
+        states.append(initial(n, seed=40 + k))
+    return params, states
+
+
+def test_ensemble_grid_classes(lib):
+    import gturbo3d_gb300 as g
+    params, _ = _class_members()
+    with g.api.Ensemble(params) as ens:
+        cls = ens.classes()
+    assert cls[0] == cls[1] == cls[2] >= 0
+    assert cls[3] == cls[4] >= 0 and cls[3] != cls[0]
+    assert cls[7] == cls[8] >= 0 and cls[7] not in (cls[0], cls[3])
+    assert cls[5] == -1 and cls[6] == -1
+
+
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("batching", [True, False])
+def test_batched_classes_match_individual_runs(lib, graph, batching):
+    """Members advanced by one launch per pass for their grid class give the
+    states and seeds of the same members stepped one by one (70 steps: a
+    64-step graph chunk and a shorter direct one)."""
+    import gturbo3d_gb300 as g
+    params, states = _class_members()
+    seeds = np.arange(300, 300 + len(params), dtype=np.int32)
+    nsteps = 70
+    refs, rseeds = [], []
+    for p, b, s in zip(params, states, seeds):
+        with g.Simulation(p) as sim:
+            sim.set_state(b)
+            rseeds.append(sim.step(nsteps, int(s)) if p.forcing else (sim.step(nsteps), int(s))[1])
+            refs.append(sim.get_state())
+    with g.api.Ensemble(params) as ens:
+        ens.set_batching(batching)
+        for i, b in enumerate(states):
+            ens.set_state(i, b)
+        out_seeds = ens.step(nsteps, seeds, graph=graph)
+        assert list(out_seeds) == rseeds
+        for i in range(len(params)):
+            assert relerr(ens.get_state(i), refs[i]) < 1e-14, i
+
+
+def test_batched_class_with_a_member_off_the_kept_set(lib):
+    """A class whose members disagree on the pruned path runs member by
+    member for that call and still matches the individual runs."""
+    import gturbo3d_gb300 as g
+    params, states = _class_members()
+    params, states = params[:3], states[:3]
+    bad = [x.copy() for x in states[1]]
+    bad[0][0, 0, 16] = 1e-4                     # kx = NX/2: outside the kept set
+    states[1] = bad
+    seeds = np.arange(5, 8, dtype=np.int32)
+    refs = []
+    for p, b, s in zip(params, states, seeds):
+        with g.Simulation(p) as sim:
+            sim.set_state(b)
+            sim.step(6, int(s))
+            refs.append(sim.get_state())
+    with g.api.Ensemble(params) as ens:
+        for i, b in enumerate(states):
+            ens.set_state(i, b)
+        ens.step(6, seeds, graph=False)
+        for i in range(3):
+            assert relerr(ens.get_state(i), refs[i]) < 1e-14, i
