@@ -123,6 +123,7 @@ class ClockSampler:
 
 
 GRID = None      # --grid NX NY NZ (profiling cases only; the default is N^3)
+TUNING = {}      # --tuning key=value (launch-shape knobs; the default run sets none)
 
 
 def make_sim(precision, device, seed_offset=0):
@@ -130,7 +131,10 @@ def make_sim(precision, device, seed_offset=0):
     nx, ny, nz = GRID if GRID else (N, N, N)
     p = g.make_params(nx, ny, nz, precision=precision, forcing="3d3c", device=device, **PHYS)
     p.famp = g.forcing_amplitude(INJECTION, p)
-    return g.Simulation(p)
+    sim = g.Simulation(p)
+    for k, v in TUNING.items():
+        sim.set_tuning(k, v)
+    return sim
 
 
 def initial_state(rank: int):
@@ -564,7 +568,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FFT, products, state); f64 exp/forcing/reductions",
             "data": "synthetic (seeded E(k) ~ k^4 exp(-2(k/3)^2) field, seed 2 + rank)",
             "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                                       **({"grid": list(GRID), "profiling_grid": True} if GRID else {})}),
+                                       **({"grid": list(GRID), "profiling_grid": True} if GRID else {}),
+                                       **({"tuning": dict(TUNING)} if TUNING else {})}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "fp64": {"value": fp64_value, "unit": UNIT, "steps": args.fp64_steps, "warmup": 3,
@@ -845,6 +850,8 @@ def main():
                     help="grid size (512 default; 1024 runs the roofline sweep's second size with nu = 8e-5)")
     ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
                     help="a non-cubic grid for profiling single kernels (the JSON line then describes it)")
+    ap.add_argument("--tuning", action="append", default=[], metavar="KEY=VALUE",
+                    help="set a launch-shape knob (gt_set_tuning) on the timed handles; repeatable")
     ap.add_argument("--workload", default="roofline", choices=["roofline", "precision", "ensemble", "adjoint"],
                     help="roofline: the headline 512^3 step (default); precision: 256^3 2D2C FP64 vs mixed; "
                          "ensemble: 64 uneven members, graph launch; adjoint: 128^3 gradient checks")
@@ -854,6 +861,9 @@ def main():
     global GRID
     N = args.size
     GRID = tuple(args.grid) if args.grid else None
+    for kv in args.tuning:
+        k, v = kv.split("=", 1)
+        TUNING[k] = int(v)
     METRIC = METRIC_FMT.format(n=N)
     if N >= 1024:
         PHYS["nu"] = 8e-5
