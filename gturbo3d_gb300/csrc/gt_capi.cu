@@ -726,7 +726,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "z_tx" && (value == 0 || value == 2 || value == 4 || value == 8 || value == 16)) h->pm.z_tx = value;
   else if (k == "x_fused" && value >= 0 && value <= 3) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
-  else if (k == "y_prefetch") h->pm.y_prefetch = value != 0;
+  else if (k == "y_prefetch" && value >= 0 && value <= 2) h->pm.y_prefetch = value;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
   else return GT_EINVAL;

@@ -173,91 +173,6 @@ template <int SIGN, typename R, typename C> __device__ __forceinline__ void dft8
   v[3] = fadd(e3, o3); v[7] = fsub(e3, o3);
 }
 
-// Shared-memory addressing of one line.
-//  Strided: element e of column x of an [L][ld] tile lives at e*ld + x.
-struct StridedIdx {
-  int ld, x;
-  __device__ __forceinline__ int operator()(int e) const { return e * ld + x; }
-};
-//  Contiguous with one padding slot every 2^sh elements (bank-conflict
-//  avoidance for the strided Stockham writes of the first stage).
-struct PaddedIdx {
-  int off, sh;
-  __device__ __forceinline__ int operator()(int e) const { return off + e + (e >> sh); }
-};
-
-// One line transform; every thread of the CTA must call this the same number
-// of times (it synchronises the CTA between stages).  The line's shared
-// scratch `sm` (addressed by `idx`) may be overwritten.
-template <int SIGN, typename R, typename Idx>
-__device__ __forceinline__ void fft_line(Cplx<R> v[8], int t, int lgL,
-                                         const Cplx<R>* __restrict__ tw, Cplx<R>* sm, Idx idx) {
-  using C = Cplx<R>;
-  const int T = 1 << (lgL - 3);
-  int rem = lgL;
-  int lgNs = 0;
-  while (true) {
-    const int lr = rem >= 3 ? 3 : rem;
-    rem -= lr;
-    const bool last = (rem == 0);
-    const int Ns = 1 << lgNs;
-    if (lr == 3) {
-      const int k = t & (Ns - 1);
-      if (lgNs > 0) {
-        const int step = k << (lgL - lgNs - 3);
-#pragma unroll
-        for (int j = 1; j < 8; ++j) v[j] = twmul<SIGN>(v[j], __ldg(&tw[j * step]));
-      }
-      dft8<SIGN, R>(v);
-      if (!last) {
-        const int base = ((t >> lgNs) << (lgNs + 3)) + k;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) sm[idx(base + (j << lgNs))] = v[j];
-      }
-    } else if (lr == 2) {
-#pragma unroll
-      for (int m = 0; m < 2; ++m) {
-        const int b = t + m * T;
-        const int k = b & (Ns - 1);
-        if (lgNs > 0) {
-          const int step = k << (lgL - lgNs - 2);
-          v[m + 2] = twmul<SIGN>(v[m + 2], __ldg(&tw[step]));
-          v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[2 * step]));
-          v[m + 6] = twmul<SIGN>(v[m + 6], __ldg(&tw[3 * step]));
-        }
-        dft4<SIGN>(v[m], v[m + 2], v[m + 4], v[m + 6]);
-        if (!last) {
-          const int base = ((b >> lgNs) << (lgNs + 2)) + k;
-#pragma unroll
-          for (int j = 0; j < 4; ++j) sm[idx(base + (j << lgNs))] = v[m + 2 * j];
-        }
-      }
-    } else {
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int b = t + m * T;
-        const int k = b & (Ns - 1);
-        if (lgNs > 0) {
-          const int step = k << (lgL - lgNs - 1);
-          v[m + 4] = twmul<SIGN>(v[m + 4], __ldg(&tw[step]));
-        }
-        dft2(v[m], v[m + 4]);
-        if (!last) {
-          const int base = ((b >> lgNs) << (lgNs + 1)) + k;
-          sm[idx(base)] = v[m];
-          sm[idx(base + Ns)] = v[m + 4];
-        }
-      }
-    }
-    if (last) break;
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = sm[idx(t + i * T)];
-    __syncthreads();
-    lgNs += lr;
-  }
-}
-
 // Offset, within the per-stage twiddle table, of the stage that starts after
 // 2^lgns points: every earlier stage but the first (radix r, Ns points
 // before it) holds (r - 1) Ns entries tw[j k L / (Ns r)] in [j - 1][k] order.

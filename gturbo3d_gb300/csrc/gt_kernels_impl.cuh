@@ -1805,9 +1805,9 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   auto middle = [&](const Geom& gs, void* const* ws) -> int {
     int rc2 = 0;
     // pass 2
-    const int ypf = pm ? pm->y_prefetch : 0;
+    const int ypf = pm ? pm->y_prefetch : 1;
     if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
-                        ypairs, (int)nm, mstride, ypf)))
+                        ypairs, (int)nm, mstride, ypf >= 1 ? 1 : 0)))
       return rc2;
     // pass 3
     if (!pm || pm->x_fused) {
@@ -1860,7 +1860,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     }
     // pass 4
     return spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs,
-                    (int)nm, mstride, ypf);
+                    (int)nm, mstride, ypf >= 2 ? 1 : 0);
   };
   if ((phases & 2) && (rc = middle(g, w))) return rc;
   // pass 5
