@@ -29,6 +29,7 @@
 // Spectral fields are [nz][ny][nhp] complex, x fastest, rows padded to a
 // multiple of 128 bytes; columns nh..nhp-1 are never read or written.
 #include <cstdio>
+#include <type_traits>
 
 #include "gt_fft.cuh"
 #include "gt_internal.h"
@@ -613,6 +614,48 @@ __device__ __forceinline__ Cplx<R> pack_c2r(const Cplx<R>* __restrict__ X1,
   return C{a.x - sg * b.y, sg * a.y + b.x};
 }
 
+// The same packing for position e = t + I N/8 of thread t of a line's N/8
+// threads, with the position's half and special cases resolved at compile
+// time: I < 4 lies below N/2 (k = e; e = 0 only for I = 0, t = 0), I = 4 is
+// N/2 + t (k = N/2 - t; the Nyquist entry for t = 0), I > 4 lies above
+// (k = N - e).  Equal to pack_c2r(X1, X2, e, N, xa).
+template <typename R, int I, int N>
+__device__ __forceinline__ Cplx<R> pack_c2r_at(const Cplx<R>* __restrict__ X1, const Cplx<R>* __restrict__ X2,
+                                               int t, int xa) {
+  using C = Cplx<R>;
+  constexpr int T = N / 8, H = N / 2;
+  if constexpr (I < 4) {
+    const int k = t + I * T;
+    if (k >= xa) return C{0, 0};
+    C a = X1[k], b = X2[k];
+    if constexpr (I == 0) {
+      if (t == 0) { a.y = 0; b.y = 0; }
+    }
+    return C{a.x - b.y, a.y + b.x};
+  } else if constexpr (I == 4) {
+    const int k = H - t;
+    if (k >= xa) return C{0, 0};
+    C a = X1[k], b = X2[k];
+    if (t == 0) { a.y = 0; b.y = 0; return C{a.x - b.y, a.y + b.x}; }
+    return C{a.x + b.y, b.x - a.y};
+  } else {
+    const int k = (8 - I) * T - t;
+    if (k >= xa) return C{0, 0};
+    const C a = X1[k], b = X2[k];
+    return C{a.x + b.y, b.x - a.y};
+  }
+}
+
+// Calls f(std::integral_constant<int, I>) for I = 0..7: a loop over the 8
+// positions of a thread whose index is a compile-time constant in the body.
+template <typename F>
+__device__ __forceinline__ void for8(F&& f) {
+  f(std::integral_constant<int, 0>{}); f(std::integral_constant<int, 1>{});
+  f(std::integral_constant<int, 2>{}); f(std::integral_constant<int, 3>{});
+  f(std::integral_constant<int, 4>{}); f(std::integral_constant<int, 5>{});
+  f(std::integral_constant<int, 6>{}); f(std::integral_constant<int, 7>{});
+}
+
 template <typename R>
 __device__ __forceinline__ Cplx<R> split_r2c(Cplx<R> a, Cplx<R> b, bool first, R s) {
   using C = Cplx<R>;
@@ -828,16 +871,15 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
 #pragma unroll 1
     for (int r = 0; r < 2; ++r) {
       const size_t row = 2 * pair + r;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int e = t + i * T;
-        v[i].a = pack_c2r<R>(reinterpret_cast<const C*>(w.p[0]) + mo + row * nhp,
-                             reinterpret_cast<const C*>(w.p[1]) + mo + row * nhp, e, N, xa);
-        v[i].b = pack_c2r<R>(reinterpret_cast<const C*>(w.p[2]) + mo + row * nhp,
-                             reinterpret_cast<const C*>(w.p[3]) + mo + row * nhp, e, N, xa);
-        v[i].c = pack_c2r<R>(reinterpret_cast<const C*>(w.p[4]) + mo + row * nhp,
-                             reinterpret_cast<const C*>(w.p[5]) + mo + row * nhp, e, N, xa);
-      }
+      const size_t ro = mo + row * nhp;
+      for8([&](auto I) {
+        v[I].a = pack_c2r_at<R, I, N>(reinterpret_cast<const C*>(w.p[0]) + ro,
+                                      reinterpret_cast<const C*>(w.p[1]) + ro, t, xa);
+        v[I].b = pack_c2r_at<R, I, N>(reinterpret_cast<const C*>(w.p[2]) + ro,
+                                      reinterpret_cast<const C*>(w.p[3]) + ro, t, xa);
+        v[I].c = pack_c2r_at<R, I, N>(reinterpret_cast<const C*>(w.p[4]) + ro,
+                                      reinterpret_cast<const C*>(w.p[5]) + ro, t, xa);
+      });
       fft_line_mem<+1, R, LGN, (sizeof(R) == 4 && !PARK)>(v, t, tw, mem, sync);
       // u = (z0.x, z0.y, z1.x), w = (z1.y, z2.x, z2.y) (produ.f90:14-16)
 #pragma unroll
