@@ -217,6 +217,12 @@ void free_handle(gt_handle* h) {
   if (h->d_count) cudaFree(h->d_count);
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_result) cudaFreeHost(h->h_result);
+  if (h->pm.stream2) {
+    cudaStreamSynchronize((cudaStream_t)h->pm.stream2);
+    cudaStreamDestroy((cudaStream_t)h->pm.stream2);
+  }
+  if (h->pm.ev_fork) cudaEventDestroy((cudaEvent_t)h->pm.ev_fork);
+  if (h->pm.ev_join) cudaEventDestroy((cudaEvent_t)h->pm.ev_join);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -455,6 +461,18 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
     }                                                \
   } while (0)
   CKH(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  {
+    // second stream and fork / join events for the overlap of the z inverse
+    // pass's k^2 half with the curl half
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ef = nullptr, ej = nullptr;
+    CKH(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    h->pm.stream2 = s2;
+    CKH(cudaEventCreateWithFlags(&ef, cudaEventDisableTiming));
+    h->pm.ev_fork = ef;
+    CKH(cudaEventCreateWithFlags(&ej, cudaEventDisableTiming));
+    h->pm.ev_join = ej;
+  }
   const size_t fbytes = g.field_elems() * h->csize;
   if (ext_fields) {
     h->fields_mem = ext_fields;
@@ -727,6 +745,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "x_fused" && value >= 0 && value <= 3) h->pm.x_fused = value;
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else if (k == "y_prefetch" && value >= 0 && value <= 2) h->pm.y_prefetch = value;
+  else if (k == "overlap") h->pm.overlap = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
   else return GT_EINVAL;
@@ -741,6 +760,7 @@ int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
   else if (k == "x_fused") *value = h->pm.x_fused;
   else if (k == "y_pairs") *value = h->pm.y_pairs;
   else if (k == "y_prefetch") *value = h->pm.y_prefetch;
+  else if (k == "overlap") *value = h->pm.overlap;
   else if (k == "fuse_stage") *value = h->pm.fuse_stage;
   else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;

@@ -130,6 +130,12 @@ struct PassTuning {
   int fuse_stage = 0;       // RK2 step: 1 = fused z forward + z inverse at the stage boundary
   int z_split = 0;          // z inverse pass: 1 = curl part and k^2 part in separate kernels;
                             // 2 = one one-region kernel, inputs read again per output line
+  int overlap = 0;          // 1 = the k^2 half of the z inverse pass and the inverse y transforms
+                            // of its three fields on a second stream, concurrently with the curl
+                            // half and the y transforms of u (needs stream2 and the two events)
+  void* stream2 = nullptr;  // the handle's second stream and the fork / join events for overlap
+  void* ev_fork = nullptr;
+  void* ev_join = nullptr;
 };
 
 // Work buffers: w[0..5] hold u_x,u_y,u_z,w_x,w_y,w_z between passes; after

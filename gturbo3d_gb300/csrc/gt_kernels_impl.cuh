@@ -1730,7 +1730,7 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
       const int TX2 = 1 << c2.lgTX;
       const int ntx2 = (xlim + TX2 - 1) / TX2;
       if (prefetch) {
-        // persistent, double-buffered: three blocks per SM
+        // persistent, double-buffered: as many blocks as fit on the device at once
         static int nsm = 0;
         if (!nsm) {
           int dev = 0;
@@ -1739,15 +1739,19 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
           if (nsm <= 0) nsm = 1;
         }
         const long long nitems = (long long)ntx2 * outer * nf * nmem;
-        const unsigned blocks = (unsigned)std::min<long long>(nitems, 3LL * nsm);
+        const int threads = c2.threads / 2, smem = 2 * c2.smem;
         GT_HOOK(kind, true);
-#define GT_L(LG)                                                                                      \
-  if (sign > 0)                                                                                       \
-    k_spass2_pf<1, LG><<<blocks, c2.threads / 2, 2 * c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, \
-                                                                   xcut0, nf, mstride, ntx2, outer, nitems); \
-  else                                                                                                \
-    k_spass2_pf<-1, LG><<<blocks, c2.threads / 2, 2 * c2.smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim,  \
-                                                                    ymask, xcut0, nf, mstride, ntx2, outer, nitems);
+#define GT_L(LG)                                                                                          \
+  {                                                                                                       \
+    auto kern = sign > 0 ? k_spass2_pf<1, LG> : k_spass2_pf<-1, LG>;                                      \
+    int per_sm = 0;                                                                                       \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess ||    \
+        per_sm < 1)                                                                                      \
+      per_sm = 1;                                                                                         \
+    const unsigned blocks = (unsigned)std::min<long long>(nitems, (long long)per_sm * nsm);              \
+    kern<<<blocks, threads, smem, s>>>(f, g, tw, ls, os, c2.lgTX - 1, xlim, ymask, xcut0, nf, mstride,   \
+                                       ntx2, outer, nitems);                                              \
+  }
         GT_DISPATCH_LG(lgL, GT_L)
 #undef GT_L
         GT_HOOK(kind, false);
@@ -1798,6 +1802,14 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
   const int ztx = pm ? pm->z_tx : 0;
+  // overlap: pass 1's k^2 half and pass 2 on the w fields run on a second stream
+  const bool ovl = (phases & 3) == 3 && pm && pm->overlap && pm->stream2 && pm->ev_fork && pm->ev_join &&
+                   pm->z_split != 2;
+  cudaStream_t s2 = ovl ? (cudaStream_t)pm->stream2 : s;
+  if (ovl) {
+    if ((rc = (int)cudaEventRecord((cudaEvent_t)pm->ev_fork, s))) return rc;
+    if ((rc = (int)cudaStreamWaitEvent(s2, (cudaEvent_t)pm->ev_fork, 0))) return rc;
+  }
   // pass 1
   if (phases & 1) {
     SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
@@ -1809,7 +1821,8 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX], nm) : dim3(c.ntiles, g.ny, nm);
     GT_HOOK(kKZinvCurl, true);
     const bool fits = c.threads / zcols<R>() <= kSpassThreads;
-    const int split = pm && pm->z_split == 1 && fits ? 1 : 0;
+    const int split = (ovl || (pm && pm->z_split == 1)) && fits ? 1 : 0;
+    if (ovl && !split) return (int)cudaErrorInvalidConfiguration;
     if (pm && pm->z_split == 2 && fits) {
       // one shared region, the input columns read again per output line
 #define GT_L(LG)                                                                                   \
@@ -1829,7 +1842,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       const dim3 grid2 = pruned ? dim3(tb.nztl[c.lgTX], 3, nm) : dim3(c.ntiles, 3, g.ny * nm);
       const int smem1 = c.smem / 3;
 #define GT_L(LG) \
-  k_zk2<R, LG><<<grid2, c.threads / zcols<R>(), smem1, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX], mstride);
+  k_zk2<R, LG><<<grid2, c.threads / zcols<R>(), smem1, s2>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX], mstride);
       GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     }
@@ -1846,11 +1859,18 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   // passes 2-4 (the y and x passes; gs and ws are the grid and work fields)
   auto middle = [&](const Geom& gs, void* const* ws) -> int {
     int rc2 = 0;
-    // pass 2
+    // pass 2 (with overlap: u on this stream, w on the second, joined before pass 3)
     const int ypf = pm ? pm->y_prefetch : 1;
-    if ((rc2 = spass<R>(gs, ws, 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
+    if ((rc2 = spass<R>(gs, ws, ovl ? 3 : 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
                         ypairs, (int)nm, mstride, ypf >= 1 ? 1 : 0)))
       return rc2;
+    if (ovl) {
+      if ((rc2 = spass<R>(gs, ws + 3, 3, tb.twy, 1, +1, s2, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
+                          ypairs, (int)nm, mstride, ypf >= 1 ? 1 : 0)))
+        return rc2;
+      if ((rc2 = (int)cudaEventRecord((cudaEvent_t)pm->ev_join, s2))) return rc2;
+      if ((rc2 = (int)cudaStreamWaitEvent(s, (cudaEvent_t)pm->ev_join, 0))) return rc2;
+    }
     // pass 3
     if (!pm || pm->x_fused) {
       // one group of nx/8 threads per row pair; as many groups per block as
