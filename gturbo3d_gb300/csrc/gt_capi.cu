@@ -223,6 +223,7 @@ void free_handle(gt_handle* h) {
   }
   if (h->pm.ev_fork) cudaEventDestroy((cudaEvent_t)h->pm.ev_fork);
   if (h->pm.ev_join) cudaEventDestroy((cudaEvent_t)h->pm.ev_join);
+  if (h->pm.ev_mid) cudaEventDestroy((cudaEvent_t)h->pm.ev_mid);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -472,6 +473,9 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
     h->pm.ev_fork = ef;
     CKH(cudaEventCreateWithFlags(&ej, cudaEventDisableTiming));
     h->pm.ev_join = ej;
+    cudaEvent_t em = nullptr;
+    CKH(cudaEventCreateWithFlags(&em, cudaEventDisableTiming));
+    h->pm.ev_mid = em;
   }
   const size_t fbytes = g.field_elems() * h->csize;
   if (ext_fields) {
@@ -746,6 +750,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "y_pairs") h->pm.y_pairs = value != 0;
   else if (k == "y_prefetch" && value >= 0 && value <= 2) h->pm.y_prefetch = value;
   else if (k == "overlap") h->pm.overlap = value != 0;
+  else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
   else return GT_EINVAL;
@@ -761,6 +766,7 @@ int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
   else if (k == "y_pairs") *value = h->pm.y_pairs;
   else if (k == "y_prefetch") *value = h->pm.y_prefetch;
   else if (k == "overlap") *value = h->pm.overlap;
+  else if (k == "slab_pipe") *value = h->pm.slab_pipe;
   else if (k == "fuse_stage") *value = h->pm.fuse_stage;
   else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;

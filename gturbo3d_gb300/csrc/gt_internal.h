@@ -133,9 +133,12 @@ struct PassTuning {
   int overlap = 0;          // 1 = the k^2 half of the z inverse pass and the inverse y transforms
                             // of its three fields on a second stream, concurrently with the curl
                             // half and the y transforms of u (needs stream2 and the two events)
-  void* stream2 = nullptr;  // the handle's second stream and the fork / join events for overlap
+  int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
+                            // two streams, the second half's y inverse after the first half's
+  void* stream2 = nullptr;  // the handle's second stream and the events for overlap / slab_pipe
   void* ev_fork = nullptr;
   void* ev_join = nullptr;
+  void* ev_mid = nullptr;
 };
 
 // Work buffers: w[0..5] hold u_x,u_y,u_z,w_x,w_y,w_z between passes; after

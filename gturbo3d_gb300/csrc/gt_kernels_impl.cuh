@@ -1857,11 +1857,11 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   const int ytx = pm && pm->y_tx ? pm->y_tx : (sizeof(R) == 4 ? (ypairs ? 8 : 4) : 0);
   const R shalf = (R)(0.5 / ((double)g.nx * g.ny * g.nz));
   // passes 2-4 (the y and x passes; gs and ws are the grid and work fields)
-  auto middle = [&](const Geom& gs, void* const* ws) -> int {
+  const int ypf = pm ? pm->y_prefetch : 1;
+  // pass 2 on stream ms (with overlap: u on ms, w on the second stream, joined before pass 3)
+  auto pass2 = [&](const Geom& gs, void* const* ws, cudaStream_t ms) -> int {
     int rc2 = 0;
-    // pass 2 (with overlap: u on this stream, w on the second, joined before pass 3)
-    const int ypf = pm ? pm->y_prefetch : 1;
-    if ((rc2 = spass<R>(gs, ws, ovl ? 3 : 6, tb.twy, 1, +1, s, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
+    if ((rc2 = spass<R>(gs, ws, ovl ? 3 : 6, tb.twy, 1, +1, ms, hook, hctx, xlim, pruned ? 1 : 0, tb.xcut, ytx,
                         ypairs, (int)nm, mstride, ypf >= 1 ? 1 : 0)))
       return rc2;
     if (ovl) {
@@ -1869,8 +1869,13 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
                           ypairs, (int)nm, mstride, ypf >= 1 ? 1 : 0)))
         return rc2;
       if ((rc2 = (int)cudaEventRecord((cudaEvent_t)pm->ev_join, s2))) return rc2;
-      if ((rc2 = (int)cudaStreamWaitEvent(s, (cudaEvent_t)pm->ev_join, 0))) return rc2;
+      if ((rc2 = (int)cudaStreamWaitEvent(ms, (cudaEvent_t)pm->ev_join, 0))) return rc2;
     }
+    return 0;
+  };
+  // passes 3 and 4 on stream ms
+  auto pass34 = [&](const Geom& gs, void* const* ws, cudaStream_t ms) -> int {
+    int rc2 = 0;
     // pass 3
     if (!pm || pm->x_fused) {
       // one group of nx/8 threads per row pair; as many groups per block as
@@ -1886,19 +1891,19 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       GT_HOOK(kKXCross, true);
       if (!pm || pm->x_fused == 2) {
 #define GT_L(LG) \
-  k_xbatch<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, 3 * smem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
+  k_xbatch<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, 3 * smem, ms>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       } else if (pm->x_fused == 3) {
         // three planes and the parking region (N complex + N real per group)
         const int psmem = 3 * smem + smem + smem / 2;
 #define GT_L(LG) \
-  k_xbatch<R, LG, true><<<dim3((unsigned)(npairs / P), nm), P * T, psmem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
+  k_xbatch<R, LG, true><<<dim3((unsigned)(npairs / P), nm), P * T, psmem, ms>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       } else {
 #define GT_L(LG) \
-  k_xfused<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, smem, s>>>(pw, gs, tb.twx, shalf, xlim, mstride);
+  k_xfused<R, LG><<<dim3((unsigned)(npairs / P), nm), P * T, smem, ms>>>(pw, gs, tb.twx, shalf, xlim, mstride);
         GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       }
@@ -1914,15 +1919,43 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       for (int i = 0; i < 6; ++i) pw.p[i] = ws[i];
       GT_HOOK(kKXCross, true);
 #define GT_L(LG) \
-  k_xcross<R, LG><<<dim3((unsigned)nblocks, nm), threads, smem, s>>>(pw, gs, tb.twx, P, shalf, xlim, mstride);
+  k_xcross<R, LG><<<dim3((unsigned)nblocks, nm), threads, smem, ms>>>(pw, gs, tb.twx, P, shalf, xlim, mstride);
       GT_DISPATCH_LG(gs.lnx, GT_L)
 #undef GT_L
       GT_HOOK(kKXCross, false);
       if ((rc2 = (int)cudaGetLastError())) return rc2;
     }
     // pass 4
-    return spass<R>(gs, ws, 3, tb.twy, 1, -1, s, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs,
+    return spass<R>(gs, ws, 3, tb.twy, 1, -1, ms, hook, hctx, xlim, pruned ? 2 : 0, tb.xcut, ytx, ypairs,
                     (int)nm, mstride, ypf >= 2 ? 1 : 0);
+  };
+  // passes 2-4 over the whole grid, or (slab_pipe) over two halves of the
+  // z-planes on two streams, the second half's y inverse transform after the
+  // first half's, so that one half's x pass runs beside the other half's y
+  // passes
+  auto middle = [&](const Geom& gs, void* const* ws) -> int {
+    const bool sp = pm && pm->slab_pipe && !ovl && pm->stream2 && pm->ev_fork && pm->ev_join &&
+                    pm->ev_mid && (gs.nz % 2) == 0 && gs.nz >= 2;
+    if (!sp) {
+      int rc2 = pass2(gs, ws, s);
+      return rc2 ? rc2 : pass34(gs, ws, s);
+    }
+    cudaStream_t t2 = (cudaStream_t)pm->stream2;
+    Geom gh = gs;
+    gh.nz = gs.nz / 2;
+    const size_t half = (size_t)gh.nz * gs.ny * gs.nhp * (size_t)csize;
+    void* wb[6];
+    for (int i = 0; i < 6; ++i) wb[i] = static_cast<char*>(ws[i]) + half;
+    int rc2;
+    if ((rc2 = (int)cudaEventRecord((cudaEvent_t)pm->ev_fork, s))) return rc2;
+    if ((rc2 = pass2(gh, ws, s))) return rc2;
+    if ((rc2 = (int)cudaEventRecord((cudaEvent_t)pm->ev_mid, s))) return rc2;
+    if ((rc2 = (int)cudaStreamWaitEvent(t2, (cudaEvent_t)pm->ev_mid, 0))) return rc2;
+    if ((rc2 = pass2(gh, wb, t2))) return rc2;
+    if ((rc2 = pass34(gh, wb, t2))) return rc2;
+    if ((rc2 = pass34(gh, ws, s))) return rc2;
+    if ((rc2 = (int)cudaEventRecord((cudaEvent_t)pm->ev_join, t2))) return rc2;
+    return (int)cudaStreamWaitEvent(s, (cudaEvent_t)pm->ev_join, 0);
   };
   if ((phases & 2) && (rc = middle(g, w))) return rc;
   // pass 5
