@@ -65,6 +65,10 @@ __device__ __forceinline__ void member_tables(const Batch<R>& bt, unsigned m, De
 }
 
 constexpr int kSmemBudget = 200 * 1024;
+// An explicitly requested tile width may use the whole per-block opt-in (227
+// KB on GB300), e.g. 16-column z tiles of three 512-row fields (216 KB, one
+// block per SM, 128-byte row segments).
+constexpr int kSmemForced = 227 * 1024;
 
 template <typename R> constexpr int max_threads() { return sizeof(R) == 8 ? 512 : 1024; }
 // Block size bound of the strided single-region passes (y passes, w = k^2 a).
@@ -1597,7 +1601,7 @@ static SCfg strided_cfg(int L, int nh, int F, int csize, int maxthreads, int for
   const int LR = strided_rows(L);   // shared-memory rows of one field (padded)
   if (force_tx > 0) {
     int TX = force_tx;
-    while (TX > 1 && (T * TX > maxthreads || F * LR * TX * csize > kSmemBudget)) TX >>= 1;
+    while (TX > 1 && (T * TX > maxthreads || F * LR * TX * csize > kSmemForced)) TX >>= 1;
     SCfg c;
     c.lgTX = ilog2i(TX);
     c.threads = T * TX;
