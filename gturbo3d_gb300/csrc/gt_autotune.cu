@@ -164,7 +164,7 @@ int gtc::autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_o
   struct Knob { int Tuning::*field; std::vector<int> values; };
   const std::vector<Knob> knobs = {{&Tuning::y_tx, {0, 4, 8}},    {&Tuning::z_tx, {0, 4, 8}},
                                    {&Tuning::x_fused, {0, 1, 2, 3}}, {&Tuning::y_pairs, {0, 1}},
-                                   {&Tuning::fuse_stage, {0, 1}}, {&Tuning::z_split, {0, 1, 2}},
+                                   {&Tuning::fuse_stage, {0, 1}}, {&Tuning::z_split, {0, 1, 2, 3}},
                                    {&Tuning::y_prefetch, {0, 1, 2}}, {&Tuning::overlap, {0, 1}},
                                    {&Tuning::slab_pipe, {0, 1}}};
   for (const Knob& k : knobs) {

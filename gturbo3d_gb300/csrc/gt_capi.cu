@@ -752,7 +752,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "overlap") h->pm.overlap = value != 0;
   else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
-  else if (k == "z_split" && value >= 0 && value <= 2) h->pm.z_split = value;
+  else if (k == "z_split" && value >= 0 && value <= 3) h->pm.z_split = value;
   else return GT_EINVAL;
   return GT_OK;
 }

@@ -262,6 +262,146 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 }
 
 // ---------------------------------------------------------------------------
+// Pass 1 as a persistent, software-pipelined kernel (z_split = 3): each block
+// walks the tile list (member-major for a batched launch) with the same three
+// shared regions as k_zinv_curl.  A tile's inputs a_0..a_2 arrive by
+// asynchronous copies into regions 0..2; each region, once the k^2 transform
+// of the previous tile has finished with it, receives the next tile's input
+// column, so neither the curl's loads nor the k^2 part's reloads stall the
+// block.  Same columns, pruning and results as k_zinv_curl.
+// ---------------------------------------------------------------------------
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(max_threads<R>() / zcols<R>())
+k_zinv_curl_pf(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const int32_t* __restrict__ tiles,
+               int per_member, int ntx, long long nitems, long long mstride) {
+  using C = Cplx<R>;
+  constexpr int W = zcols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const int reg = strided_rows(1 << LGZ) * TP;
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  auto region = [&](int c) { return sm + c * reg; };
+  // item -> the tile's row y, first column X0, column limit and element base
+  auto locate = [&](long long item, int& y, int& X0, int& ylim, size_t& base) {
+    const long long mem = item / per_member;
+    const int ti = (int)(item - mem * per_member);
+    int tile;
+    if (pruned) {
+      tile = tiles[2 * ti];
+      y = tiles[2 * ti + 1];
+    } else {
+      tile = ti % ntx;
+      y = ti / ntx;
+    }
+    X0 = tile * TX + W * xp;
+    ylim = pruned ? tb.xcut[y] : g.nh;
+    base = (size_t)y * g.nhp + (X0 < ylim ? X0 : 0) + member_offset(mstride, (unsigned)mem);
+  };
+  auto prefetch = [&](long long item, int c3) {
+    int y, X0, ylim;
+    size_t base;
+    locate(item, y, X0, ylim, base);
+    const C* ac = reinterpret_cast<const C*>(a.at(c3));
+    E* Sd = region(c3);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      const int lim = X0 < ylim ? (pruned ? tb.xcut[(size_t)z * g.ny + y] : g.nh) : 0;
+      load_cols_async<R, W>(Sd + idx(z), ac, (size_t)z * plane + base, X0, lim);
+    }
+  };
+  long long item = blockIdx.x;
+  if (item < nitems) {
+    prefetch(item, 0);
+    prefetch(item, 1);
+    prefetch(item, 2);
+  }
+  cp_async_commit();
+  for (; item < nitems; item += gridDim.x) {
+    const bool more = item + gridDim.x < nitems;
+    int y, X0, ylim;
+    size_t base;
+    locate(item, y, X0, ylim, base);
+    R kx[W], kxs[W];
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const bool in = X0 + c < ylim;
+      kx[c] = in ? tb.fkx[X0 + c] : (R)0;
+      kxs[c] = in ? tb.fkxs[X0 + c] : (R)0;
+    }
+    const R ky = tb.fky[y], kys = tb.fkys[y];
+    cp_async_wait(0);   // this thread's copies of the tile's inputs have landed
+    E v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      E ax = region(0)[idx(z)], ay = region(1)[idx(z)], az = region(2)[idx(z)];
+      const R kz = tb.fkz[z];
+      E ux, uy, uz;
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const C px = col(ax, c), py = col(ay, c), pz = col(az, c);
+        col(ux, c) = C{-ky * pz.y + kz * py.y, ky * pz.x - kz * py.x};
+        col(uy, c) = C{-kz * px.y + kx[c] * pz.y, kz * px.x - kx[c] * pz.x};
+        col(uz, c) = C{-kx[c] * py.y + ky * px.y, kx[c] * py.x - ky * px.x};
+      }
+      v[i] = ux;
+      region(1)[idx(z)] = uy;   // this thread's own slots, read just above
+      region(2)[idx(z)] = uz;
+    }
+    __syncthreads();   // every thread has read its inputs before the exchanges overwrite region 0
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+      E* S = region(f);
+      if (f > 0) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+        __syncthreads();
+      }
+      fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+      prefetch(item, f);   // the k^2 part's input a_f, into the region the transform has finished with
+      cp_async_commit();
+      C* out = reinterpret_cast<C*>(w.at(f));
+#pragma unroll
+      for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+    }
+#pragma unroll 1
+    for (int c3 = 0; c3 < 3; ++c3) {
+      E* S = region(c3);
+      cp_async_wait(2);   // a_c3 has landed (the two later groups may still be in flight)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int z = t + i * T;
+        E av = S[idx(z)];
+        const R kzs = tb.fkzs[z];
+#pragma unroll
+        for (int c = 0; c < W; ++c) {
+          const R k2 = (kxs[c] + kys) + kzs;
+          const C q = col(av, c);
+          col(av, c) = C{k2 * q.x, k2 * q.y};
+        }
+        v[i] = av;
+      }
+      __syncthreads();
+      fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+      if (more) prefetch(item + gridDim.x, c3);   // the next tile's a_c3
+      cp_async_commit();
+      C* out = reinterpret_cast<C*>(w.at(3 + c3));
+#pragma unroll
+      for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+    }
+    if constexpr (LGZ == 3) __syncthreads();   // one-stage transforms have no barrier of their own
+  }
+  cp_async_wait(0);   // nothing in flight at exit
+}
+
+// ---------------------------------------------------------------------------
 // Pass 1's w = k^2 a on its own (nlt.f90:26-40): per (x-tile, y) column block
 // of the tile list and field f = blockIdx.y, the scaled field's inverse z
 // transform with one shared region, so that more blocks are resident than in
@@ -1660,10 +1800,11 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 16 + 1];
+  cudaError_t es[8 * 17 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
+  es[n++] = allow_smem(k_zinv_curl_pf<R, LG>, optin);    \
   es[n++] = allow_smem(k_zk2<R, LG>, optin);             \
   es[n++] = allow_smem(k_zinv_curl1<R, LG>, optin);      \
   es[n++] = allow_smem(k_spass<R, 1, LG>, optin);        \
@@ -1805,10 +1946,17 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   const long long mstride = bb.nmem > 0 ? bb.mstride : 0;
   cudaStream_t s = (cudaStream_t)stream;
   const int csize = sizeof(Cplx<R>);
-  const int ztx = pm ? pm->z_tx : 0;
+  // z tiles: 16 columns (128-byte row segments, one block of three 512-row
+  // fields per SM) for FP32 z columns of 256 points or more, where they
+  // measured faster (z forward pass 0.465 -> 0.437 ms at 512^3); else the
+  // default width of strided_cfg
+  const int ztx = pm && pm->z_tx ? pm->z_tx : (sizeof(R) == 4 && g.lnz >= 8 ? 16 : 0);
+  // pass 1's tile shape (three fields per tile)
+  const SCfg c1 = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
   // overlap: pass 1's k^2 half and pass 2 on the w fields run on a second stream
+  // (only where the k^2 half fits its one-region kernel)
   const bool ovl = (phases & 3) == 3 && pm && pm->overlap && pm->stream2 && pm->ev_fork && pm->ev_join &&
-                   pm->z_split != 2;
+                   pm->z_split != 2 && pm->z_split != 3 && c1.threads / zcols<R>() <= kSpassThreads;
   cudaStream_t s2 = ovl ? (cudaStream_t)pm->stream2 : s;
   if (ovl) {
     if ((rc = (int)cudaEventRecord((cudaEvent_t)pm->ev_fork, s))) return rc;
@@ -1816,7 +1964,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
   }
   // pass 1
   if (phases & 1) {
-    SCfg c = strided_cfg(g.nz, g.nh, 3, csize, max_threads<R>(), ztx);
+    const SCfg c = c1;
     if (c.lgTX < zcols<R>() - 1) return (int)cudaErrorInvalidConfiguration;   // a column pair per thread
     if (c.lgTX < 0 || c.lgTX > 10) return (int)cudaErrorInvalidConfiguration;   // no tile list
     Ptr6 pa{}, pw{};
@@ -1827,7 +1975,32 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     const bool fits = c.threads / zcols<R>() <= kSpassThreads;
     const int split = (ovl || (pm && pm->z_split == 1)) && fits ? 1 : 0;
     if (ovl && !split) return (int)cudaErrorInvalidConfiguration;
-    if (pm && pm->z_split == 2 && fits) {
+    if (pm && pm->z_split == 3 && !ovl) {
+      // persistent, software-pipelined: as many blocks as fit on the device at once
+      static int nsm = 0;
+      if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+      }
+      const int per_member = pruned ? tb.nztl[c.lgTX] : c.ntiles * g.ny;
+      const long long nitems = (long long)per_member * nm;
+      const int threads = c.threads / zcols<R>();
+#define GT_L(LG)                                                                                         \
+  {                                                                                                      \
+    int per_sm = 0;                                                                                      \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zinv_curl_pf<R, LG>, threads, c.smem) != \
+            cudaSuccess ||                                                                               \
+        per_sm < 1)                                                                                      \
+      per_sm = 1;                                                                                        \
+    const unsigned blocks = (unsigned)std::min<long long>(nitems, (long long)per_sm * nsm);             \
+    k_zinv_curl_pf<R, LG><<<blocks, threads, c.smem, s>>>(pa, pw, tb, g, c.lgTX, pruned, tb.ztl[c.lgTX],   \
+                                                          per_member, c.ntiles, nitems, mstride);       \
+  }
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else if (pm && pm->z_split == 2 && fits) {
       // one shared region, the input columns read again per output line
 #define GT_L(LG)                                                                                   \
   k_zinv_curl1<R, LG><<<grid, c.threads / zcols<R>(), c.smem / 3, s>>>(pa, pw, tb, g, c.lgTX, pruned, \

@@ -200,7 +200,8 @@ int gt_set_pruning(gt_handle* h, int32_t enable);
 /* *active = 1 if the next gt_rk2_step takes the pruned path. */
 int gt_pruning_active(gt_handle* h, int32_t* active);
 /* Launch-shape tuning (results are unchanged):
- * "y_tx", "z_tx" (0 = default, or 2/4/8/16: x-columns per block of the y / z passes),
+ * "y_tx", "z_tx" (0 = default, or 2/4/8/16: x-columns per block of the y / z passes;
+ * the z default is 16 for FP32 z columns of 256 points or more, else 8),
  * "x_fused" (x pass: 2 = one thread group per row pair, the three packed lines
  * of a row transformed together, u x w in registers (default); 3 = the same
  * with row 0's products parked in shared memory, three resident blocks per SM
@@ -218,7 +219,9 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * term's z forward pass and the second term's z inverse pass as one kernel that
  * keeps the stage value c on chip, or two passes with c in HBM), "z_split" (z inverse
  * pass: 0 = one three-region kernel; 1 = w = k^2 a in its own one-region kernel;
- * 2 = one one-region kernel that reads the input columns again per output line). */
+ * 2 = one one-region kernel that reads the input columns again per output line;
+ * 3 = the three-region kernel made persistent, each tile's inputs copied
+ * asynchronously while the previous tile is transformed). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */

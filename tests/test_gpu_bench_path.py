@@ -102,7 +102,7 @@ def test_as_built_dt2_on_512_lines(lib, precision):
 
 
 VARIANTS = [dict(x_fused=0), dict(x_fused=1), dict(x_fused=2), dict(x_fused=3), dict(fuse_stage=1),
-            dict(z_split=1), dict(z_split=2), dict(y_pairs=0), dict(y_tx=4, z_tx=4), dict(y_tx=16, z_tx=16),
+            dict(z_split=1), dict(z_split=2), dict(z_split=3), dict(z_split=3, z_tx=4), dict(y_pairs=0), dict(y_tx=4, z_tx=4), dict(y_tx=16, z_tx=16),
             dict(fuse_stage=1, z_tx=4, y_tx=2), dict(y_prefetch=0), dict(y_prefetch=2),
             dict(y_prefetch=2, y_tx=4), dict(y_prefetch=2, y_pairs=0), dict(overlap=1),
             dict(overlap=1, fuse_stage=1), dict(overlap=1, y_prefetch=0, z_tx=4), dict(slab_pipe=1),
