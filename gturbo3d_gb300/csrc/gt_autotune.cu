@@ -24,7 +24,8 @@ using namespace gtc;
 
 Tuning gtc::get_tuning(const gt_handle* h) {
   return Tuning{h->pm.y_tx,       h->pm.z_tx,    h->pm.x_fused,    h->pm.y_pairs,
-                h->pm.fuse_stage, h->pm.z_split, h->pm.y_prefetch, h->pm.overlap, h->pm.slab_pipe};
+                h->pm.fuse_stage, h->pm.z_split, h->pm.y_prefetch, h->pm.overlap, h->pm.slab_pipe,
+                h->pm.zf_pipe};
 }
 
 void gtc::put_tuning(gt_handle* h, const Tuning& t) {
@@ -37,6 +38,7 @@ void gtc::put_tuning(gt_handle* h, const Tuning& t) {
   h->pm.y_prefetch = t.y_prefetch;
   h->pm.overlap = t.overlap;
   h->pm.slab_pipe = t.slab_pipe;
+  h->pm.zf_pipe = t.zf_pipe;
 }
 
 std::string gtc::tuning_key(const gt_handle* h) {
@@ -70,7 +72,8 @@ bool cache_lookup(const char* path, const std::string& key, Tuning& t) {
     if (get("\"y_tx\": ", u.y_tx) && get("\"z_tx\": ", u.z_tx) && get("\"x_fused\": ", u.x_fused) &&
         get("\"y_pairs\": ", u.y_pairs) && get("\"fuse_stage\": ", u.fuse_stage) &&
         get("\"z_split\": ", u.z_split) && get("\"y_prefetch\": ", u.y_prefetch) &&
-        get("\"overlap\": ", u.overlap) && get("\"slab_pipe\": ", u.slab_pipe)) {
+        get("\"overlap\": ", u.overlap) && get("\"slab_pipe\": ", u.slab_pipe) &&
+        get("\"zf_pipe\": ", u.zf_pipe)) {
       t = u;
       found = true;   // the last matching line wins
     }
@@ -86,9 +89,9 @@ void cache_store(const char* path, const std::string& key, const Tuning& t, doub
   std::fprintf(f,
                "{\"key\": \"%s\", \"y_tx\": %d, \"z_tx\": %d, \"x_fused\": %d, "
                "\"y_pairs\": %d, \"fuse_stage\": %d, \"z_split\": %d, \"y_prefetch\": %d, "
-               "\"overlap\": %d, \"slab_pipe\": %d, \"ms_per_step\": %.6f}\n",
+               "\"overlap\": %d, \"slab_pipe\": %d, \"zf_pipe\": %d, \"ms_per_step\": %.6f}\n",
                key.c_str(), t.y_tx, t.z_tx, t.x_fused, t.y_pairs, t.fuse_stage, t.z_split, t.y_prefetch,
-               t.overlap, t.slab_pipe, ms);
+               t.overlap, t.slab_pipe, t.zf_pipe, ms);
   std::fclose(f);
 }
 
@@ -166,7 +169,7 @@ int gtc::autotune_handle(gt_handle* h, const char* cache_path, double* best_ms_o
                                    {&Tuning::x_fused, {0, 1, 2, 3}}, {&Tuning::y_pairs, {0, 1}},
                                    {&Tuning::fuse_stage, {0, 1}}, {&Tuning::z_split, {0, 1, 2, 3}},
                                    {&Tuning::y_prefetch, {0, 1, 2}}, {&Tuning::overlap, {0, 1}},
-                                   {&Tuning::slab_pipe, {0, 1}}};
+                                   {&Tuning::slab_pipe, {0, 1}}, {&Tuning::zf_pipe, {0, 1}}};
   for (const Knob& k : knobs) {
     for (int v : k.values) {
       if (best.*(k.field) == v) continue;

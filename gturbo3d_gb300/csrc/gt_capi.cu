@@ -751,6 +751,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "y_prefetch" && value >= 0 && value <= 2) h->pm.y_prefetch = value;
   else if (k == "overlap") h->pm.overlap = value != 0;
   else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
+  else if (k == "zf_pipe") h->pm.zf_pipe = value != 0;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 3) h->pm.z_split = value;
   else return GT_EINVAL;
@@ -767,6 +768,7 @@ int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
   else if (k == "y_prefetch") *value = h->pm.y_prefetch;
   else if (k == "overlap") *value = h->pm.overlap;
   else if (k == "slab_pipe") *value = h->pm.slab_pipe;
+  else if (k == "zf_pipe") *value = h->pm.zf_pipe;
   else if (k == "fuse_stage") *value = h->pm.fuse_stage;
   else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;

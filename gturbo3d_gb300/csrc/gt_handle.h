@@ -108,7 +108,7 @@ int create_handle(const gt_params* p, gt_handle** out, void* ext_fields);
 
 // Launch-shape knobs the autotuner searches.
 struct Tuning {
-  int y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split, y_prefetch, overlap, slab_pipe;
+  int y_tx, z_tx, x_fused, y_pairs, fuse_stage, z_split, y_prefetch, overlap, slab_pipe, zf_pipe;
 };
 
 Tuning get_tuning(const gt_handle* h);

@@ -133,6 +133,8 @@ struct PassTuning {
   int overlap = 0;          // 1 = the k^2 half of the z inverse pass and the inverse y transforms
                             // of its three fields on a second stream, concurrently with the curl
                             // half and the y transforms of u (needs stream2 and the two events)
+  int zf_pipe = 0;          // 1 = the z forward pass persistent, the next tile's inputs copied
+                            // asynchronously behind the current tile's epilogue
   int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
                             // two streams, the second half's y inverse after the first half's
   void* stream2 = nullptr;  // the handle's second stream and the events for overlap / slab_pipe

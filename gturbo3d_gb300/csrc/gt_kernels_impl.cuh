@@ -1077,59 +1077,18 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// Pass 5: forward z transform of three fields, then the spectral epilogue.
-// ---------------------------------------------------------------------------
-template <typename R, int LGZ>
-__global__ void __launch_bounds__(max_threads<R>() / zfwd_cols<R>())
-k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
-           const int32_t* __restrict__ tiles, Batch<R> bt) {
+// The spectral epilogue of pass 5 (nlt.f90:67-81, produ.f90:83-99,
+// trunc.f90:14-28, rkstep.f90:30-48 / 86-104) at one thread's own positions
+// of a z tile: the transformed fields are in the three shared regions `reg`
+// apart, the state b(t) is read from global memory.
+template <typename R, int LGZ, int W>
+__device__ __forceinline__ void zfwd_epilogue(const ColT<R, W>* __restrict__ sm, int reg, const StridedIdxLg& idx,
+                                              int t, int X0, int y, int ylim, size_t base, size_t plane,
+                                              const Ptr6& bc, const Ptr6& out, const DevTables<R>& tb,
+                                              const Geom& g, int mode, int pruned) {
   using C = Cplx<R>;
-  constexpr int W = zfwd_cols<R>();
   using E = ColT<R, W>;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  E* sm = reinterpret_cast<E*>(smraw);
-  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
-  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
-  int tile = blockIdx.x, y = blockIdx.y;
-  if (pruned) {
-    tile = tiles[2 * blockIdx.x];
-    y = tiles[2 * blockIdx.x + 1];
-  }
-  const int X0 = tile * TX + W * xp;
-  const int ylim = pruned ? tb.xcut[y] : g.nh;
-  const bool valid = X0 < ylim;
   constexpr int T = 1 << (LGZ - 3);
-  const size_t plane = (size_t)g.ny * g.nhp;
-  const unsigned mem = pruned ? blockIdx.y : blockIdx.z;
-  member_tables(bt, mem, tb);
-  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(bt.mstride, mem);
-  const int reg = strided_rows(1 << LGZ) * TP;
-  const StridedIdxLg idx{lgTP, xp};
-  const C* tw = reinterpret_cast<const C*>(tb.twz);
-  E v[8];
-  // all three fields' columns are copied asynchronously into their regions
-  // at once (one commit group per field), so the loads of fields 1 and 2 run
-  // behind the transform of field 0
-  for (int f = 0; f < 3; ++f) {
-    const C* in = reinterpret_cast<const C*>(w.at(f));
-    E* S = sm + f * reg;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      load_cols_async<R, W>(S + idx(t + i * T), in, (size_t)(t + i * T) * plane + base, X0, ylim);
-    cp_async_commit();
-  }
-  for (int f = 0; f < 3; ++f) {
-    E* S = sm + f * reg;
-    cp_async_wait(2 - f);   // this thread's copies of field f have landed
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
-    __syncthreads();        // every thread holds its inputs before the exchanges overwrite the region
-    fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
-  }
-  if (!valid) return;  // no barrier follows
   const R ky = tb.fky[y], kys = tb.fkys[y];
   const C* b0p = reinterpret_cast<const C*>(bc.p[0]);
   const C* b1p = reinterpret_cast<const C*>(bc.p[1]);
@@ -1204,6 +1163,149 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
     store_cols<R, W>(o2, o, X0, wlim, res2);
   }
 }
+
+// ---------------------------------------------------------------------------
+// Pass 5: forward z transform of three fields, then the spectral epilogue.
+// ---------------------------------------------------------------------------
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(max_threads<R>() / zfwd_cols<R>())
+k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mode, int pruned,
+           const int32_t* __restrict__ tiles, Batch<R> bt) {
+  using C = Cplx<R>;
+  constexpr int W = zfwd_cols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
+  }
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const unsigned mem = pruned ? blockIdx.y : blockIdx.z;
+  member_tables(bt, mem, tb);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(bt.mstride, mem);
+  const int reg = strided_rows(1 << LGZ) * TP;
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  E v[8];
+  // all three fields' columns are copied asynchronously into their regions
+  // at once (one commit group per field), so the loads of fields 1 and 2 run
+  // behind the transform of field 0
+  for (int f = 0; f < 3; ++f) {
+    const C* in = reinterpret_cast<const C*>(w.at(f));
+    E* S = sm + f * reg;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      load_cols_async<R, W>(S + idx(t + i * T), in, (size_t)(t + i * T) * plane + base, X0, ylim);
+    cp_async_commit();
+  }
+  for (int f = 0; f < 3; ++f) {
+    E* S = sm + f * reg;
+    cp_async_wait(2 - f);   // this thread's copies of field f have landed
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+    __syncthreads();        // every thread holds its inputs before the exchanges overwrite the region
+    fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+  }
+  if (!valid) return;  // no barrier follows
+  zfwd_epilogue<R, LGZ, W>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned);
+}
+
+// Pass 5 as a persistent kernel (zf_pipe = 1): each block walks the tile list
+// (member-major for a batched launch).  The epilogue reads only a thread's own
+// shared slots, so as soon as a thread has finished it, the thread copies the
+// next tile's three input columns into those same slots (cp.async); the
+// barrier before the next tile's first exchange orders them after every
+// thread's epilogue.  The next tile's loads thus run behind the current
+// tile's epilogue.  Same columns, pruning and results as k_zfwd_epi.
+template <typename R, int LGZ>
+__global__ void __launch_bounds__(max_threads<R>() / zfwd_cols<R>())
+k_zfwd_epi_pf(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb0, Geom g, int lgTX, int mode, int pruned,
+              const int32_t* __restrict__ tiles, Batch<R> bt, int per_member, int ntx, long long nitems) {
+  using C = Cplx<R>;
+  constexpr int W = zfwd_cols<R>();
+  using E = ColT<R, W>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  constexpr int T = 1 << (LGZ - 3);
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const int reg = strided_rows(1 << LGZ) * TP;
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb0.twz);
+  auto locate = [&](long long item, unsigned& mem, int& y, int& X0, int& ylim, size_t& base) {
+    mem = (unsigned)(item / per_member);
+    const int ti = (int)(item - (long long)mem * per_member);
+    int tile;
+    if (pruned) {
+      tile = tiles[2 * ti];
+      y = tiles[2 * ti + 1];
+    } else {
+      tile = ti % ntx;
+      y = ti / ntx;
+    }
+    X0 = tile * TX + W * xp;
+    ylim = pruned ? tb0.xcut[y] : g.nh;
+    base = (size_t)y * g.nhp + (X0 < ylim ? X0 : 0) + member_offset(bt.mstride, mem);
+  };
+  auto prefetch = [&](long long item) {
+    unsigned mem;
+    int y, X0, ylim;
+    size_t base;
+    locate(item, mem, y, X0, ylim, base);
+    for (int f = 0; f < 3; ++f) {
+      const C* in = reinterpret_cast<const C*>(w.at(f));
+      E* S = sm + f * reg;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        load_cols_async<R, W>(S + idx(t + i * T), in, (size_t)(t + i * T) * plane + base, X0, ylim);
+      cp_async_commit();
+    }
+  };
+  long long item = blockIdx.x;
+  if (item < nitems) {
+    prefetch(item);
+  } else {
+    cp_async_commit(); cp_async_commit(); cp_async_commit();
+  }
+  for (; item < nitems; item += gridDim.x) {
+    unsigned mem;
+    int y, X0, ylim;
+    size_t base;
+    locate(item, mem, y, X0, ylim, base);
+    DevTables<R> tb = tb0;
+    member_tables(bt, mem, tb);
+    E v[8];
+    for (int f = 0; f < 3; ++f) {
+      E* S = sm + f * reg;
+      cp_async_wait(2 - f);   // this thread's copies of field f have landed
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+      __syncthreads();        // every thread holds its inputs (and has left the previous epilogue)
+      fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+    }
+    if (X0 < ylim) zfwd_epilogue<R, LGZ, W>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned);
+    if (item + gridDim.x < nitems) {
+      prefetch(item + gridDim.x);   // into this thread's own slots, which its epilogue has finished with
+    } else {
+      cp_async_commit(); cp_async_commit(); cp_async_commit();
+    }
+  }
+  cp_async_wait(0);   // nothing in flight at exit
+}
+
 
 // ---------------------------------------------------------------------------
 // Passes 5 and 1 of the RK2 step fused at the stage boundary: the forward z
@@ -1800,7 +1902,7 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 17 + 1];
+  cudaError_t es[8 * 18 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
@@ -1819,6 +1921,7 @@ static int set_smem_attrs() {
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG, true>, optin);    \
   es[n++] = allow_smem(k_zfwd_epi<R, LG>, optin);        \
+  es[n++] = allow_smem(k_zfwd_epi_pf<R, LG>, optin);     \
   es[n++] = allow_smem(k_zfwd_zinv<R, LG>, optin);       \
   es[n++] = allow_smem(k_xc2r<R, LG>, optin);            \
   es[n++] = allow_smem(k_xr2c<R, LG>, optin);
@@ -2148,11 +2251,38 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     }
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX], nm) : dim3(c.ntiles, g.ny, nm);
     GT_HOOK(kKZFwdEpi, true);
+    if (pm && pm->zf_pipe) {
+      // persistent: as many blocks as fit on the device at once
+      static int nsm = 0;
+      if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+      }
+      const int per_member = pruned ? tb.nztl[c.lgTX] : c.ntiles * g.ny;
+      const long long nitems = (long long)per_member * nm;
+      const int threads = c.threads / zfwd_cols<R>();
+#define GT_L(LG)                                                                                          \
+  {                                                                                                       \
+    int per_sm = 0;                                                                                       \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zfwd_epi_pf<R, LG>, threads, c.smem) !=  \
+            cudaSuccess ||                                                                                \
+        per_sm < 1)                                                                                       \
+      per_sm = 1;                                                                                         \
+    const unsigned blocks = (unsigned)std::min<long long>(nitems, (long long)per_sm * nsm);              \
+    k_zfwd_epi_pf<R, LG><<<blocks, threads, c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, pruned,        \
+                                                         tb.ztl[c.lgTX], bb, per_member, c.ntiles, nitems); \
+  }
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else {
 #define GT_L(LG)                                                                                   \
   k_zfwd_epi<R, LG><<<grid, c.threads / zfwd_cols<R>(), c.smem, s>>>(pw, pb, po, tb, g, c.lgTX, mode, \
                                                                  pruned, tb.ztl[c.lgTX], bb);
-    GT_DISPATCH_LG(g.lnz, GT_L)
+      GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
+    }
     GT_HOOK(kKZFwdEpi, false);
     if ((rc = (int)cudaGetLastError())) return rc;
   }

@@ -215,7 +215,9 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * transforms of its three fields on a second stream of the handle,
  * concurrently with the curl half and the y transforms of u),
  * "slab_pipe" (0/1: the y inverse, x and y passes over two halves of the
- * z-planes on two streams, the second half's y inverse after the first's), "fuse_stage" (0/1: the first nonlinear
+ * z-planes on two streams, the second half's y inverse after the first's),
+ * "zf_pipe" (0/1: the z forward pass persistent, each thread copying the next
+ * tile's inputs into its own shared slots once its epilogue is done), "fuse_stage" (0/1: the first nonlinear
  * term's z forward pass and the second term's z inverse pass as one kernel that
  * keeps the stage value c on chip, or two passes with c in HBM), "z_split" (z inverse
  * pass: 0 = one three-region kernel; 1 = w = k^2 a in its own one-region kernel;

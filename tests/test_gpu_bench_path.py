@@ -106,7 +106,8 @@ VARIANTS = [dict(x_fused=0), dict(x_fused=1), dict(x_fused=2), dict(x_fused=3), 
             dict(fuse_stage=1, z_tx=4, y_tx=2), dict(y_prefetch=0), dict(y_prefetch=2),
             dict(y_prefetch=2, y_tx=4), dict(y_prefetch=2, y_pairs=0), dict(overlap=1),
             dict(overlap=1, fuse_stage=1), dict(overlap=1, y_prefetch=0, z_tx=4), dict(slab_pipe=1),
-            dict(slab_pipe=1, y_prefetch=0, x_fused=2)]
+            dict(slab_pipe=1, y_prefetch=0, x_fused=2), dict(zf_pipe=1), dict(zf_pipe=1, z_tx=4),
+            dict(zf_pipe=1, z_split=3)]
 
 
 @pytest.mark.parametrize("tuning", VARIANTS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
