@@ -84,6 +84,7 @@ struct DevTables {
   const void* twx;      // twiddles exp(-2 pi i m / nx), m < nx  (complex R)
   const void* twy;      // ny
   const void* twz;      // nz
+  const void* twzh;     // nz / 2 (the half-length z transforms of the cluster-pair z passes)
   R omega, dt, dt2, scale;  // scale = 1/(nx ny nz)
   int truncate;
   // Truncation-aware pruning (truncate = 1 and a state that is zero outside
@@ -137,6 +138,9 @@ struct PassTuning {
                             // asynchronously behind the current tile's epilogue
   int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
                             // two streams, the second half's y inverse after the first half's
+  int z_cluster = 0;        // FP32: 1 = the z forward pass on cluster pairs of CTAs, each holding half
+                            // of a tile's z-rows (two tiles per SM; the default for z columns of 1024
+                            // points or more); 0 = one CTA per tile
   void* stream2 = nullptr;  // the handle's second stream and the events for overlap / slab_pipe
   void* ev_fork = nullptr;
   void* ev_join = nullptr;

@@ -28,6 +28,8 @@
 // nonzero (tile lists for the z passes, kx < xa for the y and x passes).
 // Spectral fields are [nz][ny][nhp] complex, x fastest, rows padded to a
 // multiple of 128 bytes; columns nh..nhp-1 are never read or written.
+#include <cooperative_groups.h>
+#include <algorithm>
 #include <cstdio>
 #include <type_traits>
 
@@ -1081,14 +1083,17 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
 // trunc.f90:14-28, rkstep.f90:30-48 / 86-104) at one thread's own positions
 // of a z tile: the transformed fields are in the three shared regions `reg`
 // apart, the state b(t) is read from global memory.
-template <typename R, int LGZ, int W>
+// Thread position e = t + i T of the tile is mode z = zmul e + zadd (zmul = 2,
+// zadd = r for the half of a cluster pair that owns the modes z = r mod 2;
+// T = 2^(LGT - 3) threads per line).
+template <typename R, int LGT, int W>
 __device__ __forceinline__ void zfwd_epilogue(const ColT<R, W>* __restrict__ sm, int reg, const StridedIdxLg& idx,
                                               int t, int X0, int y, int ylim, size_t base, size_t plane,
                                               const Ptr6& bc, const Ptr6& out, const DevTables<R>& tb,
-                                              const Geom& g, int mode, int pruned) {
+                                              const Geom& g, int mode, int pruned, int zmul = 1, int zadd = 0) {
   using C = Cplx<R>;
   using E = ColT<R, W>;
-  constexpr int T = 1 << (LGZ - 3);
+  constexpr int T = 1 << (LGT - 3);
   const R ky = tb.fky[y], kys = tb.fkys[y];
   const C* b0p = reinterpret_cast<const C*>(bc.p[0]);
   const C* b1p = reinterpret_cast<const C*>(bc.p[1]);
@@ -1098,14 +1103,15 @@ __device__ __forceinline__ void zfwd_epilogue(const ColT<R, W>* __restrict__ sm,
   C* o2 = reinterpret_cast<C*>(out.p[2]);
 #pragma unroll 2
   for (int i = 0; i < 8; ++i) {
-    const int z = t + i * T;
+    const int e = t + i * T;
+    const int z = zmul * e + zadd;
     const int zlim = tb.xcut[(size_t)z * g.ny + y];      // kept modes of this row: X < zlim
     // columns whose result is written: all of the row's columns, or only the
     // kept ones when pruned (zero outside K in both the state and the result)
     const int wlim = pruned ? zlim : ylim;
     if (X0 >= wlim) continue;
     const size_t o = (size_t)z * plane + base;
-    E n0 = sm[idx(z)], n1 = sm[reg + idx(z)], n2 = sm[2 * reg + idx(z)];
+    E n0 = sm[idx(e)], n1 = sm[reg + idx(e)], n2 = sm[2 * reg + idx(e)];
     E bb0 = load_cols<R, W>(b0p, o, X0, wlim), bb1 = load_cols<R, W>(b1p, o, X0, wlim),
       bb2 = load_cols<R, W>(b2p, o, X0, wlim);
     const R kz = tb.fkz[z], kzs = tb.fkzs[z];
@@ -1218,6 +1224,91 @@ k_zfwd_epi(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<R> tb, Geom g, int lgTX, int mod
   }
   if (!valid) return;  // no barrier follows
   zfwd_epilogue<R, LGZ, W>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 5 on a cluster pair of CTAs (FP32, z_cluster = 1).  CTA r of the pair
+// holds z-rows [r H, r H + H) (H = nz / 2) of the tile's three fields, half
+// the shared memory of k_zfwd_epi, so that two CTAs of different tiles share
+// an SM and one's loads and stores run while the other transforms (one
+// 16-column tile per SM leaves the SM idle on memory while it transforms, and
+// idle on arithmetic while it loads).  The first radix-2 stage of the length-
+// nz forward transform (decimation in frequency) pairs row e of CTA 0 with
+// row e of CTA 1: y0_e = x_e + x_{e+H} gives the even modes, y1_e =
+// (x_e - x_{e+H}) W_nz^e the odd ones; each CTA reads the other's half from
+// distributed shared memory, transforms its own with the length-H line
+// transform and runs the epilogue for its modes z = 2 k + r.  The tile list,
+// columns, pruning and epilogue are those of k_zfwd_epi.
+// ---------------------------------------------------------------------------
+// Two adjacent columns per thread (CTAs of up to 256 threads).
+template <int LGZ>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kSpassThreads, 2)
+k_zfwd_cl(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int lgTX, int mode, int pruned,
+          const int32_t* __restrict__ tiles, Batch<float> bt) {
+  using R = float;
+  using C = float2;
+  constexpr int W = 2;
+  using E = CPair<float>;
+  constexpr int LGH = LGZ - 1, H = 1 << LGH, T = H / 8;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int TX = 1 << lgTX, lgTP = lgTX - (W - 1), TP = 1 << lgTP;
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  const unsigned pair = blockIdx.x >> 1;
+  int tile = (int)pair, y = blockIdx.y;
+  if (pruned) {
+    tile = tiles[2 * pair];
+    y = tiles[2 * pair + 1];
+  }
+  const int X0 = tile * TX + W * xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const unsigned mem = pruned ? blockIdx.y : blockIdx.z;
+  member_tables(bt, mem, tb);
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0) + member_offset(bt.mstride, mem);
+  const int reg = strided_rows(H) * TP;
+  const StridedIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  const C* twh = reinterpret_cast<const C*>(tb.twzh);
+  // this CTA's rows r H + e of the three fields
+  for (int f = 0; f < 3; ++f) {
+    const C* in = reinterpret_cast<const C*>(w.at(f));
+    E* S = sm + f * reg;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = t + i * T;
+      load_cols_async<R, W>(S + idx(e), in, (size_t)(r * H + e) * plane + base, X0, ylim);
+    }
+  }
+  cp_async_commit();
+  cp_async_wait(0);
+  __syncthreads();
+  cluster.sync();   // both halves are in shared memory
+  E v[8];
+  for (int f = 0; f < 3; ++f) {
+    E* S = sm + f * reg;
+    const E* P = cluster.map_shared_rank(S, r ^ 1);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = t + i * T;
+      const E a = S[idx(e)], b = P[idx(e)];
+      if (r == 0) {
+        v[i] = cadd(a, b);                      // x_e + x_{e+H}
+      } else {
+        v[i] = twmul<-1>(csub(b, a), tw[e]);    // (x_e - x_{e+H}) W_nz^e
+      }
+    }
+    cluster.sync();   // both CTAs have read region f before either transform overwrites it
+    fft_line_ct<-1, R, LGH>(v, t, twh, S, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+  }
+  // no access to the other CTA's shared memory follows the last cluster barrier
+  if (!valid) return;
+  zfwd_epilogue<R, LGH, W>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned, 2, r);
 }
 
 // Pass 5 as a persistent kernel (zf_pipe = 1): each block walks the tile list
@@ -1902,7 +1993,7 @@ static int set_smem_attrs() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  cudaError_t es[8 * 18 + 1];
+  cudaError_t es[8 * 24 + 1];
   int n = 0;
 #define GT_ALLOW(LG)                                     \
   es[n++] = allow_smem(k_zinv_curl<R, LG>, optin);       \
@@ -1916,6 +2007,7 @@ static int set_smem_attrs() {
     es[n++] = allow_smem(k_spass2<-1, LG>, optin);       \
     es[n++] = allow_smem(k_spass2_pf<1, LG>, optin);     \
     es[n++] = allow_smem(k_spass2_pf<-1, LG>, optin);    \
+    es[n++] = allow_smem(k_zfwd_cl<(LG >= 4 ? LG : 4)>, optin); \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
@@ -2251,7 +2343,26 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     }
     const dim3 grid = pruned ? dim3(tb.nztl[c.lgTX], nm) : dim3(c.ntiles, g.ny, nm);
     GT_HOOK(kKZFwdEpi, true);
-    if (pm && pm->zf_pipe) {
+    // cluster pairs (z_cluster; the default for FP32 z columns of 1024 points
+    // or more, where the one-CTA tiles are 8 columns wide: 4.68 -> 4.31 ms at
+    // 1024^3; at 512^3 the 16-column one-CTA tiles are faster, 0.43 against
+    // 0.47 ms): tiles of up to 16 columns whose CTAs ((tile / 2) column pairs
+    // x nz / 16 threads) fit kSpassThreads
+    const int lgcl = std::min(4, 13 - g.lnz);
+    if (sizeof(R) == 4 && pm && pm->z_cluster && !pm->zf_pipe && g.lnz >= 4 && lgcl >= 1) {
+      const int TPc = 1 << (lgcl - 1), Hc = g.nz / 2;
+      const int threads = TPc * (Hc / 8);
+      const int smem = 3 * strided_rows(Hc) * TPc * 2 * csize;
+      const int ntx = (g.nh + (1 << lgcl) - 1) >> lgcl;
+      const dim3 gridc = pruned ? dim3(2 * tb.nztl[lgcl], nm) : dim3(2 * ntx, g.ny, nm);
+      const auto& tbf = reinterpret_cast<const DevTables<float>&>(tb);
+      const auto& btf = reinterpret_cast<const Batch<float>&>(bb);
+#define GT_L(LG)                                                                                         \
+  k_zfwd_cl<(LG >= 4 ? LG : 4)><<<gridc, threads, smem, s>>>(pw, pb, po, tbf, g, lgcl, mode, pruned,     \
+                                                             tb.ztl[lgcl], btf);
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else if (pm && pm->zf_pipe) {
       // persistent: as many blocks as fit on the device at once
       static int nsm = 0;
       if (!nsm) {

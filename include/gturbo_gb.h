@@ -223,7 +223,10 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * pass: 0 = one three-region kernel; 1 = w = k^2 a in its own one-region kernel;
  * 2 = one one-region kernel that reads the input columns again per output line;
  * 3 = the three-region kernel made persistent, each tile's inputs copied
- * asynchronously while the previous tile is transformed). */
+ * asynchronously while the previous tile is transformed), "z_cluster" (mixed
+ * form, 0/1: the z forward pass on thread-block cluster pairs, each CTA
+ * holding half of a tile's z-rows and the pair's first radix-2 stage read
+ * across them; the default for z columns of 1024 points or more). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */
