@@ -492,6 +492,13 @@ def run_ours(args):
     prof_steps = max(5, min(args.steps, 20))
     ms_prof, _, prof, _ = time_steps(sim, prof_steps, 1, seed, torch, profile=True)
 
+    # the DRAM rate of each pass's access pattern (copy kernels with the pass's
+    # tile shape and bytes, gt_probe_patterns), the ceiling its rate is read against
+    try:
+        patt = sim.probe_patterns() if pruned else None
+    except Exception as ex:   # a report, not the measurement
+        patt = {"error": str(ex)[:200]}
+
     # --- e2e through the C-ABI with host buffers ------------------------------
     e2e_value = None
     if not args.no_e2e:
@@ -562,6 +569,18 @@ def run_ours(args):
                 "kernels": {k: {"launches": v[0], "ms_total": v[1],
                                 "gbs": (pbytes[k] * v[0] / (v[1] / 1e3) / 1e9) if k in pbytes else None}
                             for k, v in prof.items()}}
+        if patt and "error" not in patt:
+            # per pass: the copy rate of its access pattern, and the pass's rate as a fraction of it
+            for k, pms in patt.items():
+                if k in roof["kernels"] and k in pbytes and pms > 0:
+                    pg = pbytes[k] / (pms / 1e3) / 1e9
+                    kg = roof["kernels"][k]["gbs"]
+                    roof["kernels"][k]["pattern_gbs"] = pg
+                    roof["kernels"][k]["frac_of_pattern"] = kg / pg if kg else None
+            roof["pattern_probe"] = ("gt_probe_patterns: copy kernels moving each pass's algorithmic bytes "
+                                     "with its tile shape, no arithmetic (ms per launch, 3 launches)")
+        elif patt:
+            roof["pattern_probe"] = patt
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,

@@ -87,6 +87,7 @@ SIGNATURES = {
     "gt_pruning_active": (C.c_int, [_vp, _ip]),
     "gt_selftest_wait_timeout": (C.c_int, [_vp]),
     "gt_probe_alu": (C.c_int, [C.c_int32, _dp]),
+    "gt_probe_patterns": (C.c_int, [_vp, _dp]),
     "gt_set_tuning": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
     "gt_get_tuning": (C.c_int, [_vp, C.c_char_p, _ip]),
     "gt_autotune": (C.c_int, [_vp, C.c_char_p, _dp]),

@@ -318,6 +318,16 @@ class Simulation:
         check(self.lib.gt_get_tuning(self.h, key.encode(), C.byref(v)), f"gt_get_tuning({key})")
         return v.value
 
+    PATTERN_PASSES = ("zinv_curl", "yinv", "xcross", "yfwd", "zfwd_epilogue")
+
+    def probe_patterns(self) -> dict:
+        """Milliseconds per launch of copy kernels with each pass's access
+        pattern and algorithmic bytes (gt_probe_patterns), keyed like the
+        bench's pass names.  Overwrites the work and stage buffers, not the state."""
+        r = np.zeros(5)
+        check(self.lib.gt_probe_patterns(self.h, _dp(r)), "gt_probe_patterns")
+        return dict(zip(self.PATTERN_PASSES, (float(x) for x in r)))
+
     def set_pruning(self, enable: bool) -> None:
         check(self.lib.gt_set_pruning(self.h, 1 if enable else 0), "gt_set_pruning")
 

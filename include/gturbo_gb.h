@@ -328,6 +328,17 @@ int gt_selftest_wait_timeout(gt_handle* h);
  * its roofline denominators.  No reference counterpart. */
 int gt_probe_alu(int32_t device, double* rates);
 
+/* Measures the DRAM rate that each pass's access pattern allows: copy kernels
+ * that move exactly the algorithmic bytes of the z inverse, y inverse, x, y
+ * forward and z forward passes of the handle's grid (the truncation-pruned
+ * layout) with the passes' tile shapes and none of their arithmetic.  ms[0..4]
+ * receive the milliseconds per launch, in that order; a pass's rate divided by
+ * its pattern's rate says how far the pass is from the memory system's limit
+ * for that pattern.  Overwrites the handle's work and stage buffers (not the
+ * state).  GT_EINVAL when the pruned passes are not in use (untruncated or off
+ * the kept set).  No reference counterpart. */
+int gt_probe_patterns(gt_handle* h, double* ms);
+
 /* ---- introspection ------------------------------------------------------- */
 const char* gt_strerror(int code);
 /* Text of the last CUDA failure seen on the calling thread ("" if none). */

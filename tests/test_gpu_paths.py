@@ -70,3 +70,27 @@ def test_bounded_wait_times_out_and_handle_survives(lib):
         a.step(2, 0)
         b.step(2, 0)
         assert relerr(a.get_state(), b.get_state()) == 0.0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_pattern_probe_leaves_the_trajectory_unchanged(lib, precision):
+    """gt_probe_patterns times copy kernels in the handle's work and stage
+    buffers only: a run interrupted by the probe between two steps is bitwise
+    the run without it, and every pass gets a positive time."""
+    import gturbo3d_gb300 as g
+    n = (64, 32, 32)
+    gp, _ = configs(n, precision=precision, forcing="3d3c", dt2_mode="rk2")
+    gp.famp = g.forcing_amplitude(0.1, gp)
+    b0 = initial(n, seed=9)
+    with g.Simulation(gp) as a, g.Simulation(gp) as b:
+        a.set_state(b0)
+        sa = a.step(2, 4242)
+        b.set_state(b0)
+        sb = b.step(1, 4242)
+        ms = b.probe_patterns()
+        sb = b.step(1, sb)
+        assert sa == sb
+        assert set(ms) == set(g.Simulation.PATTERN_PASSES)
+        assert all(v > 0 for v in ms.values())
+        for x, y in zip(a.get_state(), b.get_state()):
+            assert np.array_equal(x, y)
