@@ -219,6 +219,7 @@ void free_handle(gt_handle* h) {
   if (h->d_count) cudaFree(h->d_count);
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_result) cudaFreeHost(h->h_result);
+  if (h->h_flag) cudaFreeHost(h->h_flag);
   if (h->pm.stream2) {
     cudaStreamSynchronize((cudaStream_t)h->pm.stream2);
     cudaStreamDestroy((cudaStream_t)h->pm.stream2);
@@ -253,9 +254,13 @@ int rk2_nlts(gt_handle* h, int pruned) {
 
 // Reads (and clears) the device error flag of the bounded waits.
 int check_device_flag(gt_handle* h) {
-  int v = 0;
-  CK(cudaMemcpyAsync(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(h->h_flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  return take_device_flag(h);
+}
+
+int take_device_flag(gt_handle* h) {
+  const int v = *h->h_flag;
   if (v) {
     CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     g_last_error = "a bounded device wait timed out";
@@ -502,6 +507,7 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   CKH(cudaMalloc(&h->d_partials, (size_t)(h->npartials + 1) * sizeof(double)));
   CKH(cudaMalloc(&h->d_result, (size_t)h->nresult * sizeof(double)));
   CKH(cudaMallocHost(&h->h_result, (size_t)h->nresult * sizeof(double)));
+  CKH(cudaMallocHost(&h->h_flag, sizeof(int)));
   for (int i = 0; i < 2; ++i) CKH(cudaEventCreateWithFlags(&h->force_copied[i], cudaEventDisableTiming));
   CKH(cudaMalloc(&h->d_count, sizeof(unsigned long long)));
   CKH(cudaMalloc(&h->d_err, sizeof(int)));
@@ -660,7 +666,7 @@ int gt_energy(gt_handle* h, double* energy_xyz) {
   if (!h || !energy_xyz) return GT_EINVAL;
   int rc = set_dev(h);
   if (rc) return rc;
-  const int nblk = diag_blocks(h->g);
+  const int nblk = h->npartials / 3;          // the reduction's block count is capped by the partials
   const int pr = use_pruning(h) ? 1 : 0;   // state zero outside the kept set
   if (h->mixed)
     CKI(launch_energy<float>(h->g, h->t32, h->b, pr, h->d_partials, nblk, h->d_result, h->stream,
@@ -670,9 +676,11 @@ int gt_energy(gt_handle* h, double* energy_xyz) {
                               hook_fn, h));
   CK(cudaMemcpyAsync(h->h_result, h->d_result, 3 * sizeof(double), cudaMemcpyDeviceToHost,
                      h->stream));
+  // the device error flag comes back with the result, under the same synchronisation
+  CK(cudaMemcpyAsync(h->h_flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int c = 0; c < 3; ++c) energy_xyz[c] = h->h_result[c];
-  return check_device_flag(h);
+  return take_device_flag(h);
 }
 
 int gt_fft_dir(gt_handle* h, const double* real_in, double* spec_out) {

@@ -61,6 +61,7 @@ struct gt_handle {
   int npartials = 0;
   double* d_result = nullptr;
   double* h_result = nullptr;
+  int* h_flag = nullptr;       // pinned: the device error flag read back with the results
   int nresult = 0;
   int64_t launches = 0;
   // truncation-aware pruning: allowed by the caller, the state is zero outside
@@ -91,6 +92,8 @@ int nlt(gt_handle* h, void* const a[3], void* const bcor[3], void* const out[3],
 int rk2_nlts(gt_handle* h, int pruned);
 // Reads and clears the device error flag of the bounded waits.
 int check_device_flag(gt_handle* h);
+// The same for a flag already copied into h->h_flag and synchronised.
+int take_device_flag(gt_handle* h);
 // The truncation-aware pruned passes apply (allowed, truncating, state and
 // forcing inside the kept set).
 bool use_pruning(const gt_handle* h);

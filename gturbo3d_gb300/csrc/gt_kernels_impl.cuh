@@ -1873,32 +1873,49 @@ template <typename R>
 __global__ void __launch_bounds__(kDiagThreads)
 k_energy(Ptr6 bb, DevTables<R> tb, Geom g, int pruned, double* partials) {
   using C = Cplx<R>;
+  constexpr int W = 16 / (int)sizeof(C);   // complex values per 16-byte lane load
+  struct alignas(16) U {
+    C v[W];
+  };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double e0 = 0.0, e1 = 0.0, e2 = 0.0;
   const size_t rows = (size_t)g.ny * g.nz;
-  const int nwarps = gridDim.x * 8;
-  for (size_t row = (size_t)blockIdx.x * 8 + warp; row < rows; row += nwarps) {
+  const int nwarps = gridDim.x * (kDiagThreads / 32);
+  for (size_t row = (size_t)blockIdx.x * (kDiagThreads / 32) + warp; row < rows; row += nwarps) {
     const int y = (int)(row % g.ny), z = (int)(row / g.ny);
     const R ky = tb.fky[y], kz = tb.fkz[z];
     // pruned: the state is zero outside the kept prefix of the row, whose
     // terms would add exact zeros to the same partial sums
     const int xend = pruned ? tb.xcut[row] : g.nh;
-    for (int X = lane; X < xend; X += 32) {
-      const size_t o = row * g.nhp + X;
-      const C b0 = reinterpret_cast<const C*>(bb.p[0])[o];
-      const C b1 = reinterpret_cast<const C*>(bb.p[1])[o];
-      const C b2 = reinterpret_cast<const C*>(bb.p[2])[o];
-      const R kx = tb.fkx[X];
-      const R ux0 = -ky * b2.y + kz * b1.y, uy0 = ky * b2.x - kz * b1.x;
-      const R ux1 = -kz * b0.y + kx * b2.y, uy1 = kz * b0.x - kx * b2.x;
-      const R ux2 = -kx * b1.y + ky * b0.y, uy2 = kx * b1.x - ky * b0.x;
-      const double fac = (X == 0 || X == g.nh - 1) ? 0.5 : 1.0;   // k = 0 gives u = 0
-      e0 += fac * (double)(ux0 * ux0 + uy0 * uy0);
-      e1 += fac * (double)(ux1 * ux1 + uy1 * uy1);
-      e2 += fac * (double)(ux2 * ux2 + uy2 * uy2);
+    // a lane's few terms of the row are summed in the working precision, and
+    // that sum is added to the FP64 accumulators once per row
+    R s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll 3
+    for (int X0 = W * lane; X0 < xend; X0 += 32 * W) {
+      const size_t o = row * g.nhp + X0;   // X0 + W <= nhp: whole 16-byte units of the padded row
+      const U u0 = *reinterpret_cast<const U*>(reinterpret_cast<const C*>(bb.p[0]) + o);
+      const U u1 = *reinterpret_cast<const U*>(reinterpret_cast<const C*>(bb.p[1]) + o);
+      const U u2 = *reinterpret_cast<const U*>(reinterpret_cast<const C*>(bb.p[2]) + o);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const int X = X0 + c;
+        if (X >= xend) break;
+        const C b0 = u0.v[c], b1 = u1.v[c], b2 = u2.v[c];
+        const R kx = tb.fkx[X];
+        const R ux0 = -ky * b2.y + kz * b1.y, uy0 = ky * b2.x - kz * b1.x;
+        const R ux1 = -kz * b0.y + kx * b2.y, uy1 = kz * b0.x - kx * b2.x;
+        const R ux2 = -kx * b1.y + ky * b0.y, uy2 = kx * b1.x - ky * b0.x;
+        const R fac = (X == 0 || X == g.nh - 1) ? (R)0.5 : (R)1;   // k = 0 gives u = 0
+        s0 += fac * (ux0 * ux0 + uy0 * uy0);
+        s1 += fac * (ux1 * ux1 + uy1 * uy1);
+        s2 += fac * (ux2 * ux2 + uy2 * uy2);
+      }
     }
+    e0 += (double)s0;
+    e1 += (double)s1;
+    e2 += (double)s2;
   }
-  __shared__ double red[8][3];
+  __shared__ double red[kDiagThreads / 32][3];
   for (int off = 16; off > 0; off >>= 1) {
     e0 += __shfl_down_sync(0xffffffffu, e0, off);
     e1 += __shfl_down_sync(0xffffffffu, e1, off);
@@ -1908,17 +1925,30 @@ k_energy(Ptr6 bb, DevTables<R> tb, Geom g, int pruned, double* partials) {
   __syncthreads();
   if (threadIdx.x < 3) {
     double v = 0.0;
-    for (int wi = 0; wi < 8; ++wi) v += red[wi][threadIdx.x];
+    for (int wi = 0; wi < kDiagThreads / 32; ++wi) v += red[wi][threadIdx.x];
     partials[(size_t)blockIdx.x * 3 + threadIdx.x] = v;
   }
 }
 
-static __global__ void k_final_sum(const double* __restrict__ partials, int nblocks, int nq,
-                            double* __restrict__ result) {
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+// result[q] = the sum over b < nblocks of partials[b * nq + q], one block of
+// kFinalThreads per quantity: thread t adds the partials b = t, t + kFinalThreads,
+// ... in that order, then a fixed tree in shared memory adds the threads' sums,
+// so the result does not depend on scheduling.
+constexpr int kFinalThreads = 128;
+static __global__ void __launch_bounds__(kFinalThreads)
+k_final_sum(const double* __restrict__ partials, int nblocks, int nq, double* __restrict__ result) {
+  __shared__ double red[kFinalThreads];
+  for (int q = blockIdx.x; q < nq; q += gridDim.x) {
     double v = 0.0;
-    for (int b = 0; b < nblocks; ++b) v += partials[(size_t)b * nq + q];
-    result[q] = v;
+    for (int b = threadIdx.x; b < nblocks; b += kFinalThreads) v += partials[(size_t)b * nq + q];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = kFinalThreads / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) result[q] = red[0];
+    __syncthreads();
   }
 }
 
@@ -2024,6 +2054,18 @@ static int set_smem_attrs() {
     if (es[i] != cudaSuccess) return (int)es[i];
   if (dev < 32) done_mask[idx] |= 1u << dev;
   return 0;
+}
+
+// Blocks of `kernel` resident on the current device at once (one wave); 0
+// if the occupancy query fails.
+template <typename K>
+static int wave_blocks(K kernel, int threads, int smem) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess)
+    return 0;
+  return nsm * per_sm;
 }
 
 // Launches F(LG) for the run-time log2 length lg (3..10).
@@ -2574,7 +2616,7 @@ int launch_point(const Geom& g, const DevTables<R>& tb, void* const a[3], int op
   int rc = (int)cudaGetLastError();
   if (rc || op != 3) return rc;
   GT_HOOK(kKDiagFinal, true);
-  k_final_sum<<<1, 32, 0, (cudaStream_t)stream>>>(partial, bx * by, 1, partial + npartial);
+  k_final_sum<<<1, kFinalThreads, 0, (cudaStream_t)stream>>>(partial, bx * by, 1, partial + npartial);
   GT_HOOK(kKDiagFinal, false);
   return (int)cudaGetLastError();
 }
@@ -2608,7 +2650,8 @@ int launch_diag(const Geom& g, const DevTables<R>& tb, void* const b[3], void* c
   int rc = (int)cudaGetLastError();
   if (rc) return rc;
   GT_HOOK(kKDiagFinal, true);
-  k_final_sum<<<(nq + 127) / 128, 128, 0, (cudaStream_t)stream>>>(partials, nblocks, nq, result);
+  k_final_sum<<<std::max(1, std::min(nq, 1024)), kFinalThreads, 0, (cudaStream_t)stream>>>(partials, nblocks, nq,
+                                                                                        result);
   GT_HOOK(kKDiagFinal, false);
   return (int)cudaGetLastError();
 }
@@ -2618,13 +2661,18 @@ int launch_energy(const Geom& g, const DevTables<R>& tb, void* const b[3], int p
                   int nblocks, double* result, void* stream, LaunchHook hook, void* hctx) {
   Ptr6 pb{};
   for (int i = 0; i < 3; ++i) pb.p[i] = b[i];
+  // one warp per row at a time: one wave of as many blocks as are resident on
+  // the device at once (no tail wave), within the partials' capacity
+  const long long rows = (long long)g.ny * g.nz;
+  const int wave = wave_blocks(k_energy<R>, kDiagThreads, 0);
+  nblocks = (int)std::min<long long>({(rows + 7) / 8, wave > 0 ? (long long)wave : 304LL, (long long)nblocks});
   GT_HOOK(kKDiag, true);
   k_energy<R><<<nblocks, kDiagThreads, 0, (cudaStream_t)stream>>>(pb, tb, g, pruned, partials);
   GT_HOOK(kKDiag, false);
   int rc = (int)cudaGetLastError();
   if (rc) return rc;
   GT_HOOK(kKDiagFinal, true);
-  k_final_sum<<<1, 32, 0, (cudaStream_t)stream>>>(partials, nblocks, 3, result);
+  k_final_sum<<<3, kFinalThreads, 0, (cudaStream_t)stream>>>(partials, nblocks, 3, result);
   GT_HOOK(kKDiagFinal, false);
   return (int)cudaGetLastError();
 }
