@@ -224,19 +224,19 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
   };
   C* out0 = reinterpret_cast<C*>(w.p[0]);
   fft_line_ct<+1, R, LGZ>(v, t, tw, S0, idx);
-  if (k2part) prefetch(0, S0);
 #pragma unroll
   for (int i = 0; i < 8; ++i) store_cols<R, W>(out0, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+  if (k2part) prefetch(0, S0);   // behind this field's stores in the load/store queue
   for (int f = 1; f < 3; ++f) {
     E* S = f == 1 ? S1 : S2;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
     __syncthreads();
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
-    if (k2part) prefetch(f, S);
     C* out = reinterpret_cast<C*>(w.at(f));
 #pragma unroll
     for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+    if (k2part) prefetch(f, S);
   }
   if (!k2part) return;   // w = k^2 a by k_zk2 (no barrier follows)
   for (int c3 = 0; c3 < 3; ++c3) {
