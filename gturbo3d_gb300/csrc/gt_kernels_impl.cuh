@@ -2068,6 +2068,15 @@ static int wave_blocks(K kernel, int threads, int smem) {
   return nsm * per_sm;
 }
 
+// SM count of the current device (at least 1).
+static int device_sms() {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+    return 1;
+  return nsm;
+}
+
 // Launches F(LG) for the run-time log2 length lg (3..10).
 #define GT_DISPATCH_LG(lg, F)                                                  \
   switch (lg) {                                                                \
@@ -2113,13 +2122,7 @@ static int spass(const Geom& g, void* const* fields, int nf, const void* tw, int
       const int ntx2 = (xlim + TX2 - 1) / TX2;
       if (prefetch) {
         // persistent, double-buffered: as many blocks as fit on the device at once
-        static int nsm = 0;
-        if (!nsm) {
-          int dev = 0;
-          cudaGetDevice(&dev);
-          cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-          if (nsm <= 0) nsm = 1;
-        }
+        const int nsm = device_sms();   // the current device's, every launch
         const long long nitems = (long long)ntx2 * outer * nf * nmem;
         const int threads = c2.threads / 2, smem = 2 * c2.smem;
         GT_HOOK(kind, true);
@@ -2214,13 +2217,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     if (ovl && !split) return (int)cudaErrorInvalidConfiguration;
     if (pm && pm->z_split == 3 && !ovl) {
       // persistent, software-pipelined: as many blocks as fit on the device at once
-      static int nsm = 0;
-      if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm <= 0) nsm = 1;
-      }
+      const int nsm = device_sms();   // the current device's, every launch
       const int per_member = pruned ? tb.nztl[c.lgTX] : c.ntiles * g.ny;
       const long long nitems = (long long)per_member * nm;
       const int threads = c.threads / zcols<R>();
@@ -2406,13 +2403,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
 #undef GT_L
     } else if (pm && pm->zf_pipe) {
       // persistent: as many blocks as fit on the device at once
-      static int nsm = 0;
-      if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm <= 0) nsm = 1;
-      }
+      const int nsm = device_sms();   // the current device's, every launch
       const int per_member = pruned ? tb.nztl[c.lgTX] : c.ntiles * g.ny;
       const long long nitems = (long long)per_member * nm;
       const int threads = c.threads / zfwd_cols<R>();
