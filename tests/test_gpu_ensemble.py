@@ -162,3 +162,35 @@ def test_batched_class_with_a_member_off_the_kept_set(lib):
         ens.step(6, seeds, graph=False)
         for i in range(3):
             assert relerr(ens.get_state(i), refs[i]) < 1e-14, i
+
+
+def test_batched_cluster_pair_z_pass_matches_individual_runs(lib):
+    """Mixed members with 1024-point z columns run the z forward pass on
+    thread-block cluster pairs by default; one batched launch per pass for
+    their class (the member on a spare grid axis of the cluster launch) gives
+    the states of the members stepped one by one."""
+    import gturbo3d_gb300 as g
+    n = (16, 16, 1024)
+    params, states = [], []
+    for k in range(3):
+        gp, _ = configs(n, precision="mixed", forcing="3d3c", omega=2.0 + k, nu=1e-3 * (1 + k))
+        gp.famp = g.forcing_amplitude(0.1, gp)
+        params.append(gp)
+        states.append(initial(n, seed=70 + k))
+    with g.Simulation(params[0]) as sim:
+        assert sim.get_tuning("z_cluster") == 1
+    seeds = np.arange(11, 14, dtype=np.int32)
+    refs = []
+    for p, b, s in zip(params, states, seeds):
+        with g.Simulation(p) as sim:
+            sim.set_state(b)
+            sim.step(5, int(s))
+            refs.append(sim.get_state())
+    with g.api.Ensemble(params) as ens:
+        cls = ens.classes()
+        assert cls[0] == cls[1] == cls[2] >= 0
+        for i, b in enumerate(states):
+            ens.set_state(i, b)
+        ens.step(5, seeds, graph=False)
+        for i in range(3):
+            assert relerr(ens.get_state(i), refs[i]) < 1e-14, i
