@@ -516,8 +516,10 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   // (FP32, NX = 512: 1.09 against 1.12 ms); at NX = 256 and 1024 and in FP64
   // the register-resident one
   h->pm.x_fused = (h->mixed && g.lnx == 9) ? 3 : 2;
-  // z forward pass on cluster pairs for mixed z columns of 1024+ points (4.68 -> 4.31 ms at 1024^3)
+  // z forward pass on cluster pairs for mixed z columns of 1024+ points (4.68 -> 4.31 ms at 1024^3),
+  // with TMA-loaded tiles for mixed z columns of 512 points (0.435 -> 0.356 ms at 512^3; slower at 256)
   h->pm.z_cluster = (h->mixed && g.lnz >= 10) ? 1 : 0;
+  h->pm.z_tma = (h->mixed && g.lnz == 9) ? 1 : 0;
   h->state_in_k = true;   // the zero state
   h->forcing_in_k = true;
   for (size_t m = 0; m < h->ht.fix.size(); ++m) {
@@ -765,6 +767,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
   else if (k == "zf_pipe") h->pm.zf_pipe = value != 0;
   else if (k == "z_cluster" && value >= 0 && value <= 1) h->pm.z_cluster = value;
+  else if (k == "z_tma" && value >= 0 && value <= 1) h->pm.z_tma = value;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 3) h->pm.z_split = value;
   else return GT_EINVAL;
@@ -783,6 +786,7 @@ int gt_get_tuning(gt_handle* h, const char* key, int32_t* value) {
   else if (k == "slab_pipe") *value = h->pm.slab_pipe;
   else if (k == "zf_pipe") *value = h->pm.zf_pipe;
   else if (k == "z_cluster") *value = h->pm.z_cluster;
+  else if (k == "z_tma") *value = h->pm.z_tma;
   else if (k == "fuse_stage") *value = h->pm.fuse_stage;
   else if (k == "z_split") *value = h->pm.z_split;
   else return GT_EINVAL;

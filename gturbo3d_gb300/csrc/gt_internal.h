@@ -138,6 +138,9 @@ struct PassTuning {
                             // asynchronously behind the current tile's epilogue
   int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
                             // two streams, the second half's y inverse after the first half's
+  int z_tma = 0;            // FP32, z columns of up to 512 points: 1 = the z forward pass's tiles
+                            // loaded by TMA (one thread issues them, an mbarrier per field; the
+                            // default for z columns of 512 points)
   int z_cluster = 0;        // FP32: 1 = the z forward pass on cluster pairs of CTAs, each holding half
                             // of a tile's z-rows (two tiles per SM; the default for z columns of 1024
                             // points or more); 0 = one CTA per tile

@@ -35,6 +35,7 @@
 
 #include "gt_fft.cuh"
 #include "gt_internal.h"
+#include "gt_tma.cuh"
 
 namespace gt {
 
@@ -1086,8 +1087,8 @@ k_xbatch(Ptr6 w, Geom g, const void* twv, R shalf, int xa, long long mstride) {
 // Thread position e = t + i T of the tile is mode z = zmul e + zadd (zmul = 2,
 // zadd = r for the half of a cluster pair that owns the modes z = r mod 2;
 // T = 2^(LGT - 3) threads per line).
-template <typename R, int LGT, int W>
-__device__ __forceinline__ void zfwd_epilogue(const ColT<R, W>* __restrict__ sm, int reg, const StridedIdxLg& idx,
+template <typename R, int LGT, int W, typename Idx = StridedIdxLg>
+__device__ __forceinline__ void zfwd_epilogue(const ColT<R, W>* __restrict__ sm, int reg, const Idx& idx,
                                               int t, int X0, int y, int ylim, size_t base, size_t plane,
                                               const Ptr6& bc, const Ptr6& out, const DevTables<R>& tb,
                                               const Geom& g, int mode, int pruned, int zmul = 1, int zadd = 0) {
@@ -1309,6 +1310,82 @@ k_zfwd_cl(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int lgTX, int 
   // no access to the other CTA's shared memory follows the last cluster barrier
   if (!valid) return;
   zfwd_epilogue<R, LGH, W>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned, 2, r);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 5 with its tile loaded by TMA (FP32, 16-column tiles, one column per
+// thread, z_tma = 1).  One thread issues the tensor copies of the three
+// fields (boxes of 32 floats x min(nz, 256) z-rows), each field completing its
+// own mbarrier, so that field 0's transform starts as soon as its rows have
+// landed while fields 1 and 2 stream in; with per-thread cp.async copies the
+// threads spend about a quarter of a 512^3 tile issuing them.  The regions are
+// dense: a row of 16 FP32 columns is one 128-byte line, and every warp access
+// of the transforms covers whole rows, so no padding rows are needed against
+// bank conflicts.  A box also copies the columns of the tile at or beyond the
+// row's limit; those columns are transformed on their own and never stored.
+// Every wait is bounded: on a timeout the kernel raises the error flag, waits
+// once more (bounded) for its copies and finishes the tile.
+// ---------------------------------------------------------------------------
+struct DenseIdxLg {
+  int lg, x;
+  __device__ __forceinline__ int operator()(int e) const { return (e << lg) + x; }
+};
+constexpr int kZTmaLgTX = 4;   // 16 columns per tile
+
+template <int LGZ>
+__global__ void __launch_bounds__(2 << LGZ > 1024 ? 1024 : 2 << LGZ, 1)
+k_zfwd_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
+           const __grid_constant__ CUtensorMap m2, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int mode,
+           int pruned, const int32_t* __restrict__ tiles, int* err) {
+  using R = float;
+  using C = float2;
+  constexpr int W = 1;
+  constexpr int L = 1 << LGZ, T = L / 8, BOX = L < 256 ? L : 256;
+  constexpr int TX = 1 << kZTmaLgTX;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + (size_t)3 * L * TX * sizeof(C));
+  const int xp = threadIdx.x & (TX - 1), t = threadIdx.x >> kZTmaLgTX;
+  int tile = blockIdx.x, y = blockIdx.y;
+  if (pruned) {
+    tile = tiles[2 * blockIdx.x];
+    y = tiles[2 * blockIdx.x + 1];
+  }
+  const int X0 = tile * TX + xp;
+  const int ylim = pruned ? tb.xcut[y] : g.nh;
+  const bool valid = X0 < ylim;
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const int reg = L * TX;
+  const DenseIdxLg idx{kZTmaLgTX, xp};
+  if (threadIdx.x == 0) {
+    for (int f = 0; f < 3; ++f) mbar_init(&bar[f], 1);
+    fence_mbar_init();
+    const CUtensorMap* m[3] = {&m0, &m1, &m2};
+    for (int f = 0; f < 3; ++f) {
+      mbar_arrive_expect_tx(&bar[f], (uint32_t)(L * TX * sizeof(C)));
+      for (int h = 0; h < L / BOX; ++h)
+        tma_load_3d(sm + f * reg + h * BOX * TX, m[f], tile * 2 * TX, y, h * BOX, &bar[f]);
+    }
+  }
+  __syncthreads();   // the barriers are initialised before anyone waits on them
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  C v[8];
+  for (int f = 0; f < 3; ++f) {
+    C* S = sm + f * reg;
+    if (!mbar_wait(&bar[f], 0)) {   // bounded: record it, and give the copies one more bounded wait
+      raise_error(err, GT_ETIMEOUT);
+      mbar_wait(&bar[f], 0);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+    __syncthreads();   // every thread holds its inputs before the exchanges overwrite the region
+    fft_line_ct<-1, R, LGZ>(v, t, tw, S, idx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+  }
+  if (!valid) return;   // no barrier follows
+  zfwd_epilogue<R, LGZ, W, DenseIdxLg>(sm, reg, idx, t, X0, y, ylim, base, plane, bc, out, tb, g, mode, pruned);
 }
 
 // Pass 5 as a persistent kernel (zf_pipe = 1): each block walks the tile list
@@ -2038,6 +2115,7 @@ static int set_smem_attrs() {
     es[n++] = allow_smem(k_spass2_pf<1, LG>, optin);     \
     es[n++] = allow_smem(k_spass2_pf<-1, LG>, optin);    \
     es[n++] = allow_smem(k_zfwd_cl<(LG >= 4 ? LG : 4)>, optin); \
+    es[n++] = allow_smem(k_zfwd_tma<(LG >= 4 && LG <= 9 ? LG : 9)>, optin); \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
@@ -2066,6 +2144,40 @@ static int wave_blocks(K kernel, int threads, int smem) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess)
     return 0;
   return nsm * per_sm;
+}
+
+// Tensor maps of the three z forward pass inputs for TMA boxes of 32 floats
+// (16 FP32 complex columns) x 1 row x min(nz, 256) z-planes: dims {2 nhp
+// floats, ny, nz}, strides {nhp, ny nhp} complex values.  false when the
+// encoder cannot be had or refuses a map (the caller then uses cp.async).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static bool tensor_maps_zcols(const Geom& g, void* const w[6], CUtensorMap maps[3]) {
+  static EncodeTiledFn enc = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      enc = reinterpret_cast<EncodeTiledFn>(fn);
+    looked_up = true;
+  }
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * g.nhp, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.nhp * 8, (cuuint64_t)g.ny * g.nhp * 8};
+  const cuuint32_t box[3] = {32, 1, (cuuint32_t)std::min(g.nz, 256)};
+  const cuuint32_t es[3] = {1, 1, 1};
+  for (int f = 0; f < 3; ++f) {
+    if (reinterpret_cast<uintptr_t>(w[f]) % 16) return false;
+    if (enc(&maps[f], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, w[f], dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
 }
 
 // SM count of the current device (at least 1).
@@ -2388,7 +2500,23 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     // 0.47 ms): tiles of up to 16 columns whose CTAs ((tile / 2) column pairs
     // x nz / 16 threads) fit kSpassThreads
     const int lgcl = std::min(4, 13 - g.lnz);
-    if (sizeof(R) == 4 && pm && pm->z_cluster && !pm->zf_pipe && g.lnz >= 4 && lgcl >= 1) {
+    CUtensorMap zmaps[3];
+    const bool ztma = sizeof(R) == 4 && pm && pm->z_tma && nm == 1 && g.lnz >= 4 && g.lnz <= 9 &&
+                      !pm->zf_pipe && tensor_maps_zcols(g, w, zmaps);
+    if (ztma) {
+      // TMA-loaded tiles of 16 columns, one column per thread
+      const int threads = (1 << kZTmaLgTX) * (g.nz / 8);
+      const int smem = 3 * g.nz * (1 << kZTmaLgTX) * csize + 3 * (int)sizeof(uint64_t);
+      const int ntx = (g.nh + (1 << kZTmaLgTX) - 1) >> kZTmaLgTX;
+      const dim3 gridt = pruned ? dim3(tb.nztl[kZTmaLgTX]) : dim3(ntx, g.ny);
+      const auto& tbf = reinterpret_cast<const DevTables<float>&>(tb);
+#define GT_L(LG)                                                                                          \
+  k_zfwd_tma<(LG >= 4 && LG <= 9 ? LG : 9)><<<gridt, threads, smem, s>>>(zmaps[0], zmaps[1], zmaps[2], pb, po, \
+                                                                         tbf, g, mode, pruned,            \
+                                                                         tb.ztl[kZTmaLgTX], err);
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else if (sizeof(R) == 4 && pm && pm->z_cluster && !pm->zf_pipe && g.lnz >= 4 && lgcl >= 1) {
       const int TPc = 1 << (lgcl - 1), Hc = g.nz / 2;
       const int threads = TPc * (Hc / 8);
       const int smem = 3 * strided_rows(Hc) * TPc * 2 * csize;

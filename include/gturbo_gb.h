@@ -226,7 +226,10 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * asynchronously while the previous tile is transformed), "z_cluster" (mixed
  * form, 0/1: the z forward pass on thread-block cluster pairs, each CTA
  * holding half of a tile's z-rows and the pair's first radix-2 stage read
- * across them; the default for z columns of 1024 points or more). */
+ * across them; the default for z columns of 1024 points or more), "z_tma" (mixed
+ * form, 0/1: the z forward pass's tiles loaded by TMA, one thread issuing the
+ * tensor copies of the three fields with an mbarrier each; the default for z
+ * columns of 512 points). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */
