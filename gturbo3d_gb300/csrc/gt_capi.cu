@@ -155,7 +155,7 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   build_ztiles(g, ht.xcut.data(), (int)sizeof(Cplx<R>), tiles);
   if (tiles.empty()) tiles = {0, 0};
   const size_t o_tiles = put(tiles.data(), tiles.size() * sizeof(int32_t));
-  size_t o_tl[11];
+  size_t o_tl[11], o_tlzc[11];
   int n_tl[11];
   for (int lg = 0; lg < 11; ++lg) {
     std::vector<int32_t> tl;
@@ -163,6 +163,16 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
     if (tl.empty()) tl = {0, 0};
     o_tl[lg] = put(tl.data(), tl.size() * sizeof(int32_t));
     n_tl[lg] = (int)(tl.size() / 2);
+    // kept half range of each tile's first column: xcut[z][y] is non-increasing in |kz|
+    std::vector<int32_t> zc(tl.size() / 2, 0);
+    for (size_t e = 0; e < zc.size(); ++e) {
+      const int X = tl[2 * e] << lg, y = tl[2 * e + 1];
+      int z = 0;
+      while (z + 1 <= g.nz / 2 && ht.xcut[(size_t)(z + 1) * g.ny + y] > X) ++z;
+      zc[e] = z;
+    }
+    if (zc.empty()) zc = {0};
+    o_tlzc[lg] = put(zc.data(), zc.size() * sizeof(int32_t));
   }
   (void)nemk;
   void* mem = nullptr;
@@ -192,6 +202,7 @@ int upload_tables(gt_handle* h, DevTables<R>& t) {
   for (int lg = 0; lg < 11; ++lg) {
     t.ztl[lg] = dptr<const int32_t>(mem, o_tl[lg]);
     t.nztl[lg] = n_tl[lg];
+    t.ztlzc[lg] = dptr<const int32_t>(mem, o_tlzc[lg]);
   }
   t.xa = ht.xcut[0];
   return GT_OK;
@@ -516,10 +527,11 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   // (FP32, NX = 512: 1.09 against 1.12 ms); at NX = 256 and 1024 and in FP64
   // the register-resident one
   h->pm.x_fused = (h->mixed && g.lnx == 9) ? 3 : 2;
-  // z forward pass on cluster pairs for mixed z columns of 1024+ points (4.68 -> 4.31 ms at 1024^3),
-  // with TMA-loaded tiles for mixed z columns of 512 points (0.435 -> 0.356 ms at 512^3; slower at 256)
+  // z forward pass on cluster pairs for mixed z columns of 1024+ points (4.68 -> 4.31 ms at 1024^3);
+  // TMA-loaded tiles: the z forward pass for mixed z columns of 512 points (0.435 -> 0.356 ms at
+  // 512^3; slower at 256), the z inverse pass for 256 and 512 (0.549 -> 0.512 ms, 0.075 -> 0.070 ms)
   h->pm.z_cluster = (h->mixed && g.lnz >= 10) ? 1 : 0;
-  h->pm.z_tma = (h->mixed && g.lnz == 9) ? 1 : 0;
+  h->pm.z_tma = h->mixed ? ((g.lnz == 9 ? 1 : 0) | (g.lnz == 8 || g.lnz == 9 ? 2 : 0)) : 0;
   h->state_in_k = true;   // the zero state
   h->forcing_in_k = true;
   for (size_t m = 0; m < h->ht.fix.size(); ++m) {
@@ -767,7 +779,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
   else if (k == "zf_pipe") h->pm.zf_pipe = value != 0;
   else if (k == "z_cluster" && value >= 0 && value <= 1) h->pm.z_cluster = value;
-  else if (k == "z_tma" && value >= 0 && value <= 1) h->pm.z_tma = value;
+  else if (k == "z_tma" && value >= 0 && value <= 3) h->pm.z_tma = value;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 3) h->pm.z_split = value;
   else return GT_EINVAL;

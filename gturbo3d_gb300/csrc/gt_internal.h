@@ -95,6 +95,8 @@ struct DevTables {
   int nztiles;
   const int32_t* ztl[11];  // the same for every tile width 2^lg, lg = 0..10
   int nztl[11];
+  const int32_t* ztlzc[11];  // per entry of ztl[lg]: the largest z <= nz/2 whose row keeps the
+                             // tile's first column (the kept z are z <= zc and z >= nz - zc)
   int xa;
 };
 
@@ -138,9 +140,10 @@ struct PassTuning {
                             // asynchronously behind the current tile's epilogue
   int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
                             // two streams, the second half's y inverse after the first half's
-  int z_tma = 0;            // FP32, z columns of up to 512 points: 1 = the z forward pass's tiles
-                            // loaded by TMA (one thread issues them, an mbarrier per field; the
-                            // default for z columns of 512 points)
+  int z_tma = 0;            // FP32, z columns of up to 512 points, tiles loaded by TMA (one thread
+                            // issues them, an mbarrier per field): bit 1 = the z forward pass (the
+                            // default for z columns of 512 points), bit 2 = the z inverse pass (the
+                            // default for 256 and 512)
   int z_cluster = 0;        // FP32: 1 = the z forward pass on cluster pairs of CTAs, each holding half
                             // of a tile's z-rows (two tiles per SM; the default for z columns of 1024
                             // points or more); 0 = one CTA per tile

@@ -265,6 +265,161 @@ k_zinv_curl(Ptr6 a, Ptr6 w, DevTables<R> tb, Geom g, int lgTX, int pruned, const
 }
 
 // ---------------------------------------------------------------------------
+// Pass 1 with TMA-loaded inputs (FP32, pruned, 16-column tiles, z_tma bit 2).
+// The tile's kept z-rows of a_0..a_2 (z <= zc and z >= nz - zc, zc from the
+// tile list) arrive by tensor copies of 32-row boxes issued by one thread,
+// an mbarrier per field, into dense regions (16 FP32 columns make whole
+// 128-byte rows); for the k^2 part each a_c is copied again, by TMA, into the
+// region the u_c transform has finished with.  Rows a box does not cover are
+// never read: every read of an input row is masked by the row's kept prefix,
+// as the cp.async copies of k_zinv_curl zero-fill them.  Bounded waits.
+// ---------------------------------------------------------------------------
+// Dense shared tile of a TMA-loaded z pass: element e of column x of a
+// [rows][2^lg] tile (rows of 16 FP32 columns are whole 128-byte lines, so the
+// transforms' warp accesses cover whole rows and need no padding rows).
+struct DenseIdxLg {
+  int lg, x;
+  __device__ __forceinline__ int operator()(int e) const { return (e << lg) + x; }
+};
+constexpr int kZTmaLgTX = 4;   // 16 columns per tile
+constexpr int kZBoxRows = 32;
+
+template <int LGZ>
+__global__ void __launch_bounds__(1 << LGZ > 1024 ? 1024 : (1 << LGZ), 1)
+k_zinv_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
+           const __grid_constant__ CUtensorMap m2, Ptr6 w, DevTables<float> tb, Geom g,
+           const int32_t* __restrict__ tiles, const int32_t* __restrict__ tzc, int* err) {
+  using R = float;
+  using C = float2;
+  constexpr int W = 2;
+  using E = CPair<float>;
+  constexpr int L = 1 << LGZ, T = L / 8;
+  constexpr int TX = 1 << kZTmaLgTX, lgTP = kZTmaLgTX - 1, TP = TX / 2;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  E* sm = reinterpret_cast<E*>(smraw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + (size_t)3 * L * TP * sizeof(E));
+  const int xp = threadIdx.x & (TP - 1), t = threadIdx.x >> lgTP;
+  const int tile = tiles[2 * blockIdx.x], y = tiles[2 * blockIdx.x + 1];
+  const int zc = tzc[blockIdx.x];
+  // boxes: rows [0, hend) and [tstart, L), whole boxes, no overlap
+  const int hend = min(L, (zc / kZBoxRows + 1) * kZBoxRows);
+  const int tstart = max(hend, (L - zc) / kZBoxRows * kZBoxRows);
+  const int nbox = hend / kZBoxRows + (L - tstart) / kZBoxRows;
+  const int X0 = tile * TX + W * xp;
+  const int ylim = tb.xcut[y];
+  const bool valid = X0 < ylim;
+  const size_t plane = (size_t)g.ny * g.nhp;
+  const size_t base = (size_t)y * g.nhp + (valid ? X0 : 0);
+  const int reg = L * TP;
+  const DenseIdxLg idx{lgTP, xp};
+  const C* tw = reinterpret_cast<const C*>(tb.twz);
+  const CUtensorMap* m[3] = {&m0, &m1, &m2};
+  // thread 0: the kept rows of field c into region c, completing bar[k]
+  auto load_field = [&](int c, int k) {
+    mbar_arrive_expect_tx(&bar[k], (uint32_t)(nbox * kZBoxRows * TX * sizeof(C)));
+    for (int z0 = 0; z0 < hend; z0 += kZBoxRows)
+      tma_load_3d(sm + c * reg + z0 * TP, m[c], tile * 2 * TX, y, z0, &bar[k]);
+    for (int z0 = tstart; z0 < L; z0 += kZBoxRows)
+      tma_load_3d(sm + c * reg + z0 * TP, m[c], tile * 2 * TX, y, z0, &bar[k]);
+  };
+  auto wait = [&](int k) {
+    if (!mbar_wait(&bar[k], 0)) {   // bounded: record it, and give the copies one more bounded wait
+      raise_error(err, GT_ETIMEOUT);
+      mbar_wait(&bar[k], 0);
+    }
+  };
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) mbar_init(&bar[k], 1);
+    fence_mbar_init();
+    for (int c = 0; c < 3; ++c) load_field(c, c);
+  }
+  __syncthreads();   // the barriers are initialised before anyone waits on them
+  R kx[W], kxs[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const bool in = X0 + c < ylim;
+    kx[c] = in ? tb.fkx[X0 + c] : (R)0;
+    kxs[c] = in ? tb.fkxs[X0 + c] : (R)0;
+  }
+  const R ky = tb.fky[y], kys = tb.fkys[y];
+  // the value of column pair X0 at row z of region c, zero outside the row's kept prefix
+  auto kept = [&](const E* S, int z, int lim) {
+    E u = S[idx(z)];
+    if (X0 + 1 >= lim) {
+      u.b = C{0, 0};
+      if (X0 >= lim) u.a = C{0, 0};
+    }
+    return u;
+  };
+  wait(0);
+  wait(1);
+  wait(2);
+  E* S0 = sm;
+  E* S1 = sm + reg;
+  E* S2 = sm + 2 * reg;
+  E v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int z = t + i * T;
+    const int lim = valid ? tb.xcut[(size_t)z * g.ny + y] : 0;
+    E ax = kept(S0, z, lim), ay = kept(S1, z, lim), az = kept(S2, z, lim);
+    const R kz = tb.fkz[z];
+    E ux, uy, uz;
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      const C px = col(ax, c), py = col(ay, c), pz = col(az, c);
+      col(ux, c) = C{-ky * pz.y + kz * py.y, ky * pz.x - kz * py.x};
+      col(uy, c) = C{-kz * px.y + kx[c] * pz.y, kz * px.x - kx[c] * pz.x};
+      col(uz, c) = C{-kx[c] * py.y + ky * px.y, kx[c] * py.x - ky * px.x};
+    }
+    v[i] = ux;
+    S1[idx(z)] = uy;   // this thread's own slots, read just above
+    S2[idx(z)] = uz;
+  }
+  __syncthreads();   // every thread has read region 0 before the exchanges overwrite it
+  for (int f = 0; f < 3; ++f) {
+    E* S = f == 0 ? S0 : (f == 1 ? S1 : S2);
+    if (f > 0) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = S[idx(t + i * T)];
+      __syncthreads();
+    }
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.at(f));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+    // region f is free once every thread is past the transform's last exchange
+    // read: a_f again, for the k^2 part, by tensor copies behind the stores
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) load_field(f, 3 + f);
+  }
+  for (int c3 = 0; c3 < 3; ++c3) {
+    E* S = c3 == 0 ? S0 : (c3 == 1 ? S1 : S2);
+    wait(3 + c3);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int z = t + i * T;
+      const int lim = valid ? tb.xcut[(size_t)z * g.ny + y] : 0;
+      E av = kept(S, z, lim);
+      const R kzs = tb.fkzs[z];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const R k2 = (kxs[c] + kys) + kzs;
+        const C q = col(av, c);
+        col(av, c) = C{k2 * q.x, k2 * q.y};
+      }
+      v[i] = av;
+    }
+    __syncthreads();   // every thread holds its inputs before the exchanges overwrite the region
+    fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
+    C* out = reinterpret_cast<C*>(w.at(3 + c3));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Pass 1 as a persistent, software-pipelined kernel (z_split = 3): each block
 // walks the tile list (member-major for a batched launch) with the same three
 // shared regions as k_zinv_curl.  A tile's inputs a_0..a_2 arrive by
@@ -1326,11 +1481,6 @@ k_zfwd_cl(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int lgTX, int 
 // Every wait is bounded: on a timeout the kernel raises the error flag, waits
 // once more (bounded) for its copies and finishes the tile.
 // ---------------------------------------------------------------------------
-struct DenseIdxLg {
-  int lg, x;
-  __device__ __forceinline__ int operator()(int e) const { return (e << lg) + x; }
-};
-constexpr int kZTmaLgTX = 4;   // 16 columns per tile
 
 template <int LGZ>
 __global__ void __launch_bounds__(2 << LGZ > 1024 ? 1024 : 2 << LGZ, 1)
@@ -2116,6 +2266,7 @@ static int set_smem_attrs() {
     es[n++] = allow_smem(k_spass2_pf<-1, LG>, optin);    \
     es[n++] = allow_smem(k_zfwd_cl<(LG >= 4 ? LG : 4)>, optin); \
     es[n++] = allow_smem(k_zfwd_tma<(LG >= 4 && LG <= 9 ? LG : 9)>, optin); \
+    es[n++] = allow_smem(k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9)>, optin); \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
@@ -2153,7 +2304,7 @@ static int wave_blocks(K kernel, int threads, int smem) {
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-static bool tensor_maps_zcols(const Geom& g, void* const w[6], CUtensorMap maps[3]) {
+static bool tensor_maps_zcols(const Geom& g, void* const w[], CUtensorMap maps[3], int box_rows = 256) {
   static EncodeTiledFn enc = nullptr;
   static bool looked_up = false;
   if (!looked_up) {
@@ -2168,7 +2319,7 @@ static bool tensor_maps_zcols(const Geom& g, void* const w[6], CUtensorMap maps[
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)2 * g.nhp, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
   const cuuint64_t strides[2] = {(cuuint64_t)g.nhp * 8, (cuuint64_t)g.ny * g.nhp * 8};
-  const cuuint32_t box[3] = {32, 1, (cuuint32_t)std::min(g.nz, 256)};
+  const cuuint32_t box[3] = {32, 1, (cuuint32_t)std::min(g.nz, box_rows)};
   const cuuint32_t es[3] = {1, 1, 1};
   for (int f = 0; f < 3; ++f) {
     if (reinterpret_cast<uintptr_t>(w[f]) % 16) return false;
@@ -2327,7 +2478,20 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     const bool fits = c.threads / zcols<R>() <= kSpassThreads;
     const int split = (ovl || (pm && pm->z_split == 1)) && fits ? 1 : 0;
     if (ovl && !split) return (int)cudaErrorInvalidConfiguration;
-    if (pm && pm->z_split == 3 && !ovl) {
+    CUtensorMap amaps[3];
+    const bool zitma = sizeof(R) == 4 && pruned && pm && (pm->z_tma & 2) && nm == 1 && !split && !ovl &&
+                       pm->z_split == 0 && g.lnz >= 5 && g.lnz <= 9 && tensor_maps_zcols(g, a, amaps, kZBoxRows);
+    if (zitma) {
+      const int lgt = kZTmaLgTX;
+      const int threads = (1 << (lgt - 1)) * (g.nz / 8);
+      const int smem = 3 * g.nz * (1 << lgt) * csize + 6 * (int)sizeof(uint64_t);
+      const auto& tbf = reinterpret_cast<const DevTables<float>&>(tb);
+#define GT_L(LG)                                                                                          \
+  k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9)><<<dim3(tb.nztl[lgt]), threads, smem, s>>>(                      \
+      amaps[0], amaps[1], amaps[2], pw, tbf, g, tb.ztl[lgt], tb.ztlzc[lgt], err);
+      GT_DISPATCH_LG(g.lnz, GT_L)
+#undef GT_L
+    } else if (pm && pm->z_split == 3 && !ovl) {
       // persistent, software-pipelined: as many blocks as fit on the device at once
       const int nsm = device_sms();   // the current device's, every launch
       const int per_member = pruned ? tb.nztl[c.lgTX] : c.ntiles * g.ny;
@@ -2501,7 +2665,7 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
     // x nz / 16 threads) fit kSpassThreads
     const int lgcl = std::min(4, 13 - g.lnz);
     CUtensorMap zmaps[3];
-    const bool ztma = sizeof(R) == 4 && pm && pm->z_tma && nm == 1 && g.lnz >= 4 && g.lnz <= 9 &&
+    const bool ztma = sizeof(R) == 4 && pm && (pm->z_tma & 1) && nm == 1 && g.lnz >= 4 && g.lnz <= 9 &&
                       !pm->zf_pipe && tensor_maps_zcols(g, w, zmaps);
     if (ztma) {
       // TMA-loaded tiles of 16 columns, one column per thread

@@ -227,9 +227,10 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * form, 0/1: the z forward pass on thread-block cluster pairs, each CTA
  * holding half of a tile's z-rows and the pair's first radix-2 stage read
  * across them; the default for z columns of 1024 points or more), "z_tma" (mixed
- * form, 0/1: the z forward pass's tiles loaded by TMA, one thread issuing the
- * tensor copies of the three fields with an mbarrier each; the default for z
- * columns of 512 points). */
+ * form, bits: the z passes' tiles loaded by TMA, one thread issuing the tensor
+ * copies of the three fields with an mbarrier each; 1 the z forward pass, the
+ * default for z columns of 512 points; 2 the z inverse pass, the default for
+ * 256 and 512). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */
