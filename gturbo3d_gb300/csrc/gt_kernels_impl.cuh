@@ -2305,17 +2305,16 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 static bool tensor_maps_zcols(const Geom& g, void* const w[], CUtensorMap maps[3], int box_rows = 256) {
-  static EncodeTiledFn enc = nullptr;
-  static bool looked_up = false;
-  if (!looked_up) {
+  // looked up once (a function-local static: thread-safe initialisation)
+  static const EncodeTiledFn enc = [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      enc = reinterpret_cast<EncodeTiledFn>(fn);
-    looked_up = true;
-  }
+      return reinterpret_cast<EncodeTiledFn>(fn);
+    return (EncodeTiledFn) nullptr;
+  }();
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)2 * g.nhp, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
   const cuuint64_t strides[2] = {(cuuint64_t)g.nhp * 8, (cuuint64_t)g.ny * g.nhp * 8};
