@@ -30,6 +30,7 @@
 // multiple of 128 bytes; columns nh..nhp-1 are never read or written.
 #include <cooperative_groups.h>
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <type_traits>
 
@@ -2241,12 +2242,14 @@ static cudaError_t allow_smem(K kernel, int optin) {
 
 template <typename R>
 static int set_smem_attrs() {
-  static unsigned done_mask[2] = {0u, 0u};   // bit d: device d configured
+  // bit d: device d configured (atomic: handles on other host threads may configure concurrently;
+  // setting the attributes twice is harmless)
+  static std::atomic<unsigned> done_mask[2] = {{0u}, {0u}};
   const int idx = sizeof(R) == 8 ? 1 : 0;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
-  if (dev < 32 && (done_mask[idx] >> dev) & 1u) return 0;
+  if (dev < 32 && (done_mask[idx].load() >> dev) & 1u) return 0;
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
@@ -2281,7 +2284,7 @@ static int set_smem_attrs() {
   es[n++] = allow_smem(k_diag<R>, optin);
   for (int i = 0; i < n; ++i)
     if (es[i] != cudaSuccess) return (int)es[i];
-  if (dev < 32) done_mask[idx] |= 1u << dev;
+  if (dev < 32) done_mask[idx].fetch_or(1u << dev);
   return 0;
 }
 
