@@ -528,10 +528,10 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   // the register-resident one
   h->pm.x_fused = (h->mixed && g.lnx == 9) ? 3 : 2;
   // z forward pass on cluster pairs for mixed z columns of 1024+ points (4.68 -> 4.31 ms at 1024^3);
-  // TMA-loaded tiles: the z forward pass for mixed z columns of 512 points (0.435 -> 0.356 ms at
-  // 512^3; slower at 256), the z inverse pass for 256 and 512 (0.549 -> 0.512 ms, 0.075 -> 0.070 ms)
+  // TMA-loaded tiles for mixed z columns of 256 and 512 points: the z forward pass (0.435 -> 0.356 ms
+  // at 512^3, 0.061 -> 0.055 ms at 256^3) and the z inverse pass (0.549 -> 0.512, 0.075 -> 0.070 ms)
   h->pm.z_cluster = (h->mixed && g.lnz >= 10) ? 1 : 0;
-  h->pm.z_tma = h->mixed ? ((g.lnz == 9 ? 1 : 0) | (g.lnz == 8 || g.lnz == 9 ? 2 : 0)) : 0;
+  h->pm.z_tma = (h->mixed && (g.lnz == 8 || g.lnz == 9)) ? 3 : 0;
   h->state_in_k = true;   // the zero state
   h->forcing_in_k = true;
   for (size_t m = 0; m < h->ht.fix.size(); ++m) {

@@ -141,9 +141,8 @@ struct PassTuning {
   int slab_pipe = 0;        // 1 = the y inverse, x and y passes over two halves of the z-planes on
                             // two streams, the second half's y inverse after the first half's
   int z_tma = 0;            // FP32, z columns of up to 512 points, tiles loaded by TMA (one thread
-                            // issues them, an mbarrier per field): bit 1 = the z forward pass (the
-                            // default for z columns of 512 points), bit 2 = the z inverse pass (the
-                            // default for 256 and 512)
+                            // issues them, an mbarrier per field): bit 1 = the z forward pass, bit 2
+                            // = the z inverse pass (both the default for z columns of 256 and 512)
   int z_cluster = 0;        // FP32: 1 = the z forward pass on cluster pairs of CTAs, each holding half
                             // of a tile's z-rows (two tiles per SM; the default for z columns of 1024
                             // points or more); 0 = one CTA per tile

@@ -1483,8 +1483,11 @@ k_zfwd_cl(Ptr6 w, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int lgTX, int 
 // once more (bounded) for its copies and finishes the tile.
 // ---------------------------------------------------------------------------
 
+// 2 L threads per block; at most 64 registers, so that shorter lines keep as
+// many tiles per SM as their shared memory allows (two of 96 KB at L = 256).
 template <int LGZ>
-__global__ void __launch_bounds__(2 << LGZ > 1024 ? 1024 : 2 << LGZ, 1)
+__global__ void __launch_bounds__(2 << LGZ > 1024 ? 1024 : 2 << LGZ,
+                                  (2 << LGZ) >= 1024 ? 1 : (1024 / (2 << LGZ) < 4 ? 1024 / (2 << LGZ) : 4))
 k_zfwd_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
            const __grid_constant__ CUtensorMap m2, Ptr6 bc, Ptr6 out, DevTables<float> tb, Geom g, int mode,
            int pruned, const int32_t* __restrict__ tiles, int* err) {

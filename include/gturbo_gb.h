@@ -228,9 +228,8 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * holding half of a tile's z-rows and the pair's first radix-2 stage read
  * across them; the default for z columns of 1024 points or more), "z_tma" (mixed
  * form, bits: the z passes' tiles loaded by TMA, one thread issuing the tensor
- * copies of the three fields with an mbarrier each; 1 the z forward pass, the
- * default for z columns of 512 points; 2 the z inverse pass, the default for
- * 256 and 512). */
+ * copies of the three fields with an mbarrier each; 1 the z forward pass, 2
+ * the z inverse pass; both the default for z columns of 256 and 512 points). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */

@@ -85,10 +85,10 @@ def test_bench_default_x_pass_is_the_one_checked(lib):
         gp, _ = configs(n, precision=prec)
         with g.Simulation(gp) as sim:
             assert sim.get_tuning("z_cluster") == want, (n, prec)
-    # TMA-loaded z tiles: the forward pass (bit 1) for mixed z columns of 512 points, the
-    # inverse pass (bit 2) for 256 and 512
+    # TMA-loaded z tiles: the forward (bit 1) and inverse (bit 2) passes for mixed z
+    # columns of 256 and 512 points
     for n, prec, want in [((16, 16, 512), "mixed", 3), ((16, 16, 512), "fp64", 0),
-                          ((16, 16, 256), "mixed", 2), ((16, 16, 128), "mixed", 0), ((16, 8, 1024), "mixed", 0)]:
+                          ((16, 16, 256), "mixed", 3), ((16, 16, 128), "mixed", 0), ((16, 8, 1024), "mixed", 0)]:
         gp, _ = configs(n, precision=prec)
         with g.Simulation(gp) as sim:
             assert sim.get_tuning("z_tma") == want, (n, prec)
@@ -128,7 +128,7 @@ VARIANTS = [dict(x_fused=0), dict(x_fused=1), dict(x_fused=2), dict(x_fused=3), 
 @pytest.mark.parametrize("tuning", VARIANTS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
 @pytest.mark.parametrize("n,precision", [((64, 32, 32), "fp64"), ((64, 32, 32), "mixed"),
                                          ((512, 16, 16), "mixed"), ((16, 16, 512), "mixed"),
-                                         ((16, 512, 16), "fp64")])
+                                         ((16, 16, 256), "mixed"), ((16, 512, 16), "fp64")])
 def test_every_tuning_knob_against_the_oracle(lib, tuning, n, precision):
     """Each non-default launch shape checked against the oracle itself (not
     against another shape of the library), three steps."""
