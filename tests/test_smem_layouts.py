@@ -141,3 +141,32 @@ def test_strided_tiles_conflict_free(L, lgTP, esize):
     """y/z tiles at the default widths: 4 column pairs of FP32 (16-byte
     elements) or FP64 columns, and 8 FP32 columns of the z forward pass."""
     assert excess(L, esize, tile_addr(L, lgTP), (L // 8) << lgTP) == 1.0
+
+
+def dense_tile_addr(L, lgTP):
+    """Slot of a thread's element in a dense z tile of the TMA-loaded passes
+    (DenseIdxLg: e << lgTP | x, no padding rows)."""
+    TP = 1 << lgTP
+
+    def addr(th, acc):
+        x, t = th & (TP - 1), th >> lgTP
+        return (acc(th, t) << lgTP) + x
+    return addr
+
+
+@pytest.mark.parametrize("L", [64, 128, 256, 512])
+@pytest.mark.parametrize("lgTP,esize", [(4, 8), (3, 16)])
+def test_dense_16_column_tiles_conflict_free(L, lgTP, esize):
+    """The dense tiles of the TMA-loaded z passes: 16 FP32 columns, one per
+    thread (k_zfwd_tma) or in pairs (k_zinv_tma).  A row is one 128-byte line
+    and a warp's access covers whole rows, so every exchange store and load
+    takes the minimum number of wavefronts without padding rows."""
+    assert excess(L, esize, dense_tile_addr(L, lgTP), (L // 8) << lgTP) == 1.0
+
+
+@pytest.mark.parametrize("L", [64, 512])
+def test_dense_8_column_tiles_would_conflict(L):
+    """The same dense layout with 8 FP32 columns (64-byte rows) does take
+    extra wavefronts in some exchange, which is why the dense tiles are used
+    only at 16 columns and the narrower tiles keep their padding rows."""
+    assert excess(L, 8, dense_tile_addr(L, 3), (L // 8) << 3) > 1.0
