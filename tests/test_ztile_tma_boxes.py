@@ -75,3 +75,40 @@ def test_kept_rows_are_a_symmetric_interval_in_kz():
             if len(zs):
                 bound = np.abs(kz[zs]).max()
                 assert set(zs) == set(np.nonzero(np.abs(kz) <= bound)[0])
+
+
+@pytest.mark.parametrize("lnx", [4, 5, 6, 7, 8, 9, 10])
+@pytest.mark.parametrize("lnz", [4, 5, 6, 7, 8, 9])
+def test_tensor_copies_meet_the_alignment_rules(lnx, lnz):
+    """The tensor maps and boxes of both TMA z passes (tensor_maps_zcols and the
+    launches in csrc/gt_kernels_impl.cuh), restated for FP32 rows padded to
+    nhp = nh rounded up to 16 complex values: the innermost coordinate of every
+    copy, the strides and the box's inner extent are multiples of 16 bytes, every
+    box lies inside the padded row, every shared destination is 128-byte aligned,
+    and the shared tile plus its mbarriers fits the 227 KB opt-in."""
+    csize = 8                                   # FP32 complex
+    nx, nz = 1 << lnx, 1 << lnz
+    nh = nx // 2 + 1
+    align = 128 // csize
+    nhp = (nh + align - 1) // align * align
+    dims_x = 2 * nhp                            # floats
+    stride_row, stride_plane = nhp * 8, 32 * nhp * 8
+    assert stride_row % 16 == 0 and stride_plane % 16 == 0
+    box_x = 32                                  # floats: 16 complex columns
+    assert box_x * 4 % 16 == 0
+    for tile in range((nh + TX - 1) // TX):
+        x = tile * 2 * TX                       # floats
+        assert x * 4 % 16 == 0
+        assert x + box_x <= dims_x              # whole box inside the padded row
+    # z forward pass: boxes of min(nz, 256) rows at z = 0, 256, ...; region f at f * nz * 16 columns
+    zbox = min(nz, 256)
+    for f in range(3):
+        for h in range(nz // zbox):
+            assert ((f * nz + h * zbox) * TX * csize) % 128 == 0
+    assert 3 * nz * TX * csize + 3 * 8 <= 227 * 1024
+    # z inverse pass (nz >= 32): boxes of 32 rows, regions of nz rows of 8 column pairs (16 bytes each)
+    if nz >= BOX:
+        for c in range(3):
+            for z0 in range(0, nz, BOX):
+                assert ((c * nz * (TX // 2) + z0 * (TX // 2)) * 16) % 128 == 0
+        assert 3 * nz * TX * csize + 6 * 8 <= 227 * 1024
