@@ -6,9 +6,10 @@ parity tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 does.  It follows the reference Fortran line by line (citations are
 ``src/<file>.f90:<line>`` within the Gturbo3D repository).
 
-Parity status: the reference needs nvfortran + OpenACC + cuFFT and no Fortran
-compiler exists on either machine, so the reference itself cannot run here and
-it ships no golden outputs.  This restatement is pinned by known answers that
+Parity status: parity unpinned against the reference itself.  The reference
+needs nvfortran + OpenACC + cuFFT and no Fortran compiler exists on either
+machine, so it cannot run here, and it ships no tests or golden outputs.  This
+restatement is pinned instead by known answers that
 follow from the reference's own formulas (LCG sequence, forced-mode counts,
 exact single-mode FFTs, Beltrami/ABC invariance, the closed-form linear update
 of a pure-rotation mode) in ``tests/test_oracle_known_answers.py``.  The cuFFT
