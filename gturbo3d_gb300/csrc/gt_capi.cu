@@ -531,7 +531,9 @@ int gtc::create_handle(const gt_params* p, gt_handle** out, void* ext_fields) {
   // TMA-loaded tiles for mixed z columns of 256 and 512 points: the z forward pass (0.435 -> 0.356 ms
   // at 512^3, 0.061 -> 0.055 ms at 256^3) and the z inverse pass (0.549 -> 0.512, 0.075 -> 0.070 ms)
   h->pm.z_cluster = (h->mixed && g.lnz >= 10) ? 1 : 0;
-  h->pm.z_tma = (h->mixed && (g.lnz == 8 || g.lnz == 9)) ? 3 : 0;
+  // the z inverse pass's tensor stores (bit 4) only at 256 points: 0.0710 -> 0.0671 ms at 256^3,
+  // but 0.513 -> 0.518 ms at 512^3
+  h->pm.z_tma = h->mixed ? (g.lnz == 8 ? 7 : (g.lnz == 9 ? 3 : 0)) : 0;
   h->state_in_k = true;   // the zero state
   h->forcing_in_k = true;
   for (size_t m = 0; m < h->ht.fix.size(); ++m) {
@@ -779,7 +781,7 @@ int gt_set_tuning(gt_handle* h, const char* key, int32_t value) {
   else if (k == "slab_pipe") h->pm.slab_pipe = value != 0;
   else if (k == "zf_pipe") h->pm.zf_pipe = value != 0;
   else if (k == "z_cluster" && value >= 0 && value <= 1) h->pm.z_cluster = value;
-  else if (k == "z_tma" && value >= 0 && value <= 3) h->pm.z_tma = value;
+  else if (k == "z_tma" && value >= 0 && value <= 7) h->pm.z_tma = value;
   else if (k == "fuse_stage") h->pm.fuse_stage = value != 0;
   else if (k == "z_split" && value >= 0 && value <= 3) h->pm.z_split = value;
   else return GT_EINVAL;

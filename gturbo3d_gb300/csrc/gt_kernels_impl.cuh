@@ -285,11 +285,25 @@ struct DenseIdxLg {
 constexpr int kZTmaLgTX = 4;   // 16 columns per tile
 constexpr int kZBoxRows = 32;
 
-template <int LGZ>
+// Tensor maps of pass 1's six outputs, for its tensor stores.
+struct ZOutMaps {
+  CUtensorMap m[6];
+};
+
+// TST: the six outputs leave by tensor stores from the tile's regions (z_tma
+// bit 4) instead of per-thread stores.  A transformed field is written into
+// its region and one thread issues the stores; the threads go on with the next
+// transform while the stores drain, and a_c is copied again into region c for
+// the k^2 part once region c's store has read it.  The stores write whole
+// 16-column boxes: the tile's columns at or beyond the row's limit receive the
+// zeros their transforms produce, which no later pass reads (the y pass masks
+// its inputs by the same limits).
+template <int LGZ, bool TST = false>
 __global__ void __launch_bounds__(1 << LGZ > 1024 ? 1024 : (1 << LGZ), 1)
 k_zinv_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
-           const __grid_constant__ CUtensorMap m2, Ptr6 w, DevTables<float> tb, Geom g,
-           const int32_t* __restrict__ tiles, const int32_t* __restrict__ tzc, int* err) {
+           const __grid_constant__ CUtensorMap m2, const __grid_constant__ ZOutMaps om, Ptr6 w,
+           DevTables<float> tb, Geom g, const int32_t* __restrict__ tiles, const int32_t* __restrict__ tzc,
+           int* err) {
   using R = float;
   using C = float2;
   constexpr int W = 2;
@@ -378,6 +392,20 @@ k_zinv_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUten
     S2[idx(z)] = uz;
   }
   __syncthreads();   // every thread has read region 0 before the exchanges overwrite it
+  constexpr int OB = L < 256 ? L : 256;   // rows per store box
+  // thread 0: region S, all L rows, to output k by tensor stores, one bulk group
+  auto store_field = [&](const E* S, int k) {
+    for (int z0 = 0; z0 < L; z0 += OB) tma_store_3d(&om.m[k], S + z0 * TP, tile * 2 * TX, y, z0);
+    bulk_commit();
+  };
+  // every thread: its transformed column pair into region S (the transform's
+  // last exchange read is behind a barrier), ordered before the tensor stores
+  auto put = [&](E* S) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[idx(t + i * T)] = v[i];
+    fence_proxy_async_smem();
+    __syncthreads();
+  };
   for (int f = 0; f < 3; ++f) {
     E* S = f == 0 ? S0 : (f == 1 ? S1 : S2);
     if (f > 0) {
@@ -386,14 +414,25 @@ k_zinv_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUten
       __syncthreads();
     }
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
-    C* out = reinterpret_cast<C*>(w.at(f));
+    if constexpr (TST) {
+      put(S);
+      if (threadIdx.x == 0) {
+        store_field(S, f);
+        if (f > 0) {   // region f-1's store has read its source: a_{f-1} again, for the k^2 part
+          bulk_wait_read<1>();
+          load_field(f - 1, 3 + f - 1);
+        }
+      }
+    } else {
+      C* out = reinterpret_cast<C*>(w.at(f));
 #pragma unroll
-    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
-    // region f is free once every thread is past the transform's last exchange
-    // read: a_f again, for the k^2 part, by tensor copies behind the stores
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) load_field(f, 3 + f);
+      for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+      // region f is free once every thread is past the transform's last exchange
+      // read: a_f again, for the k^2 part, by tensor copies behind the stores
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) load_field(f, 3 + f);
+    }
   }
   for (int c3 = 0; c3 < 3; ++c3) {
     E* S = c3 == 0 ? S0 : (c3 == 1 ? S1 : S2);
@@ -414,9 +453,25 @@ k_zinv_tma(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUten
     }
     __syncthreads();   // every thread holds its inputs before the exchanges overwrite the region
     fft_line_ct<+1, R, LGZ>(v, t, tw, S, idx);
-    C* out = reinterpret_cast<C*>(w.at(3 + c3));
+    if constexpr (TST) {
+      put(S);
+      if (threadIdx.x == 0) {
+        store_field(S, 3 + c3);
+        if (c3 == 0) {   // the u_z store has read region 2: a_2 again
+          bulk_wait_read<1>();
+          load_field(2, 5);
+        }
+      }
+    } else {
+      C* out = reinterpret_cast<C*>(w.at(3 + c3));
 #pragma unroll
-    for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+      for (int i = 0; i < 8; ++i) store_cols<R, W>(out, (size_t)(t + i * T) * plane + base, X0, ylim, v[i]);
+    }
+  }
+  // the stores read the regions until they complete: the block (and its
+  // shared memory) stays until the issuing thread has seen them complete
+  if constexpr (TST) {
+    if (threadIdx.x == 0) bulk_wait_all();
   }
 }
 
@@ -2273,6 +2328,7 @@ static int set_smem_attrs() {
     es[n++] = allow_smem(k_zfwd_cl<(LG >= 4 ? LG : 4)>, optin); \
     es[n++] = allow_smem(k_zfwd_tma<(LG >= 4 && LG <= 9 ? LG : 9)>, optin); \
     es[n++] = allow_smem(k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9)>, optin); \
+    es[n++] = allow_smem(k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9), true>, optin); \
   }                                                      \
   es[n++] = allow_smem(k_xcross<R, LG>, optin);          \
   es[n++] = allow_smem(k_xbatch<R, LG>, optin);          \
@@ -2491,9 +2547,17 @@ static int nlt_phases(const Geom& g, const DevTables<R>& tb, void* const a[3], v
       const int threads = (1 << (lgt - 1)) * (g.nz / 8);
       const int smem = 3 * g.nz * (1 << lgt) * csize + 6 * (int)sizeof(uint64_t);
       const auto& tbf = reinterpret_cast<const DevTables<float>&>(tb);
+      // tensor stores of the six outputs (bit 4): boxes of 16 columns x min(nz, 256) rows
+      ZOutMaps om{};
+      const bool zist = (pm->z_tma & 4) && tensor_maps_zcols(g, w, om.m, 256) &&
+                        tensor_maps_zcols(g, w + 3, om.m + 3, 256);
 #define GT_L(LG)                                                                                          \
-  k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9)><<<dim3(tb.nztl[lgt]), threads, smem, s>>>(                      \
-      amaps[0], amaps[1], amaps[2], pw, tbf, g, tb.ztl[lgt], tb.ztlzc[lgt], err);
+  if (zist)                                                                                               \
+    k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9), true><<<dim3(tb.nztl[lgt]), threads, smem, s>>>(              \
+        amaps[0], amaps[1], amaps[2], om, pw, tbf, g, tb.ztl[lgt], tb.ztlzc[lgt], err);                     \
+  else                                                                                                    \
+    k_zinv_tma<(LG >= 5 && LG <= 9 ? LG : 9)><<<dim3(tb.nztl[lgt]), threads, smem, s>>>(                    \
+        amaps[0], amaps[1], amaps[2], om, pw, tbf, g, tb.ztl[lgt], tb.ztlzc[lgt], err);
       GT_DISPATCH_LG(g.lnz, GT_L)
 #undef GT_L
     } else if (pm && pm->z_split == 3 && !ovl) {

@@ -86,9 +86,9 @@ def test_bench_default_x_pass_is_the_one_checked(lib):
         with g.Simulation(gp) as sim:
             assert sim.get_tuning("z_cluster") == want, (n, prec)
     # TMA-loaded z tiles: the forward (bit 1) and inverse (bit 2) passes for mixed z
-    # columns of 256 and 512 points
+    # columns of 256 and 512 points, the inverse pass's tensor stores (bit 4) at 256
     for n, prec, want in [((16, 16, 512), "mixed", 3), ((16, 16, 512), "fp64", 0),
-                          ((16, 16, 256), "mixed", 3), ((16, 16, 128), "mixed", 0), ((16, 8, 1024), "mixed", 0)]:
+                          ((16, 16, 256), "mixed", 7), ((16, 16, 128), "mixed", 0), ((16, 8, 1024), "mixed", 0)]:
         gp, _ = configs(n, precision=prec)
         with g.Simulation(gp) as sim:
             assert sim.get_tuning("z_tma") == want, (n, prec)
@@ -122,7 +122,8 @@ VARIANTS = [dict(x_fused=0), dict(x_fused=1), dict(x_fused=2), dict(x_fused=3), 
             dict(slab_pipe=1, y_prefetch=0, x_fused=2), dict(zf_pipe=1), dict(zf_pipe=1, z_tx=4),
             dict(zf_pipe=1, z_split=3), dict(z_cluster=1), dict(z_cluster=1, fuse_stage=1),
             dict(z_cluster=1, y_prefetch=0, x_fused=2), dict(z_cluster=1, zf_pipe=1), dict(z_tma=1),
-            dict(z_tma=1, fuse_stage=1), dict(z_tma=0), dict(z_tma=2), dict(z_tma=3), dict(z_tma=3, z_tx=4)]
+            dict(z_tma=1, fuse_stage=1), dict(z_tma=0), dict(z_tma=2), dict(z_tma=3), dict(z_tma=3, z_tx=4),
+            dict(z_tma=6), dict(z_tma=7), dict(z_tma=7, fuse_stage=1), dict(z_tma=7, y_prefetch=0)]
 
 
 @pytest.mark.parametrize("tuning", VARIANTS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
