@@ -144,6 +144,7 @@ struct PassTuning {
                             // issues them, an mbarrier per field): bit 1 = the z forward pass, bit 2
                             // = the z inverse pass (both the default for z columns of 256 and 512);
                             // bit 4, with bit 2: the z inverse pass's outputs leave by TMA stores
+                            // (the default for z columns of 256)
   int z_cluster = 0;        // FP32: 1 = the z forward pass on cluster pairs of CTAs, each holding half
                             // of a tile's z-rows (two tiles per SM; the default for z columns of 1024
                             // points or more); 0 = one CTA per tile

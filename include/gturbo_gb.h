@@ -230,7 +230,8 @@ int gt_pruning_active(gt_handle* h, int32_t* active);
  * form, bits: the z passes' tiles loaded by TMA, one thread issuing the tensor
  * copies of the three fields with an mbarrier each; 1 the z forward pass, 2
  * the z inverse pass; both the default for z columns of 256 and 512 points;
- * 4, with 2, the z inverse pass's six outputs written by tensor stores). */
+ * 4, with 2, the z inverse pass's six outputs written by tensor stores, the
+ * default for z columns of 256 points). */
 int gt_set_tuning(gt_handle* h, const char* key, int32_t value);
 /* The current value of one gt_set_tuning knob (the per-grid default until
  * it is set). */
