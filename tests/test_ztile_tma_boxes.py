@@ -112,3 +112,11 @@ def test_tensor_copies_meet_the_alignment_rules(lnx, lnz):
             for z0 in range(0, nz, BOX):
                 assert ((c * nz * (TX // 2) + z0 * (TX // 2)) * 16) % 128 == 0
         assert 3 * nz * TX * csize + 6 * 8 <= 227 * 1024
+        # its tensor stores (z_tma bit 4): boxes of min(nz, 256) rows from each region,
+        # at non-negative coordinates, covering the region's rows once
+        obox = min(nz, 256)
+        for c in range(3):
+            starts = list(range(0, nz, obox))
+            assert sum(obox for _ in starts) == nz and min(starts) >= 0
+            for z0 in starts:
+                assert ((c * nz * (TX // 2) + z0 * (TX // 2)) * 16) % 128 == 0
